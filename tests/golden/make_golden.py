@@ -1,0 +1,205 @@
+"""Generate the golden fixtures in this directory from the holodeck reference.
+
+Run in a container that holds the reference sources (see ``ref_env.py``)::
+
+    python tests/golden/make_golden.py
+
+Every fixture is produced by the unmodified reference code path (plus the
+one-token Cython-3 fix and import stand-ins described in ``ref_env.py``),
+with ``holodeck.cyutils.PCG64`` replaced by a seeded ``np.random.PCG64`` so
+that realizations are reproducible.  The tests never import the reference:
+they read these ``.npz`` files.
+"""
+
+import ast
+import os
+import sys
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+warnings.filterwarnings("ignore")
+
+import ref_env  # noqa: E402
+
+holo = ref_env.import_reference()
+holo.log.setLevel(40)
+from holodeck.constants import PC, YR, GYR  # noqa: E402
+import holodeck.cyutils as cyutils  # noqa: E402
+import holodeck.sams.sam_cyutils as sam_cyutils  # noqa: E402
+from holodeck import single_sources, gravwaves  # noqa: E402
+
+
+def seed_rng(seed):
+    cyutils.PCG64 = lambda: np.random.PCG64(seed)
+
+
+def make_sam(shape, scatter_dex, phi0=-2.77, mchar0_log10=11.24, alpha0=-1.24, mamp_log10=8.69, mplaw=1.17):
+    gsmf = holo.sams.GSMF_Schechter(phi0=phi0, mchar0_log10=mchar0_log10, alpha0=alpha0)
+    gpf = holo.sams.GPF_Power_Law()
+    gmt = holo.sams.GMT_Power_Law()
+    mmb = holo.host_relations.MMBulge_KH2013(mamp_log10=mamp_log10, mplaw=mplaw, scatter_dex=scatter_dex)
+    return holo.sams.Semi_Analytic_Model(gsmf=gsmf, gpf=gpf, gmt=gmt, mmbulge=mmb, shape=shape)
+
+
+def run_path(sam, hard, fobs_gw_edges, nreals, nloud, seed):
+    """The body of ``Semi_Analytic_Model.gwb`` (sam.py:918-947), keeping intermediates."""
+    fobs_gw_cents = 0.5 * (fobs_gw_edges[1:] + fobs_gw_edges[:-1])
+    fobs_orb_edges = fobs_gw_edges / 2.0
+    fobs_orb_cents = fobs_gw_cents / 2.0
+    redz_final, dnum = sam_cyutils.dynamic_binary_number_at_fobs(fobs_orb_cents, sam, hard, holo.cosmo)
+    edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
+    number = sam_cyutils.integrate_differential_number_3dx1d(edges, dnum)
+    h2fdf = gravwaves.char_strain_sq_from_bin_edges_redz(edges, redz_final)
+    order = np.argsort(-h2fdf[..., 0].flatten())
+    seed_rng(seed)
+    hc_ss, hc_bg = single_sources.ss_gws_redz(edges, redz_final, number, realize=nreals, loudest=nloud)
+    # the full gwb() call must give the same answer with the same seed
+    seed_rng(seed)
+    hc_ss2, hc_bg2 = sam.gwb(fobs_gw_edges, hard=hard, realize=nreals, loudest=nloud)
+    assert np.array_equal(hc_ss, hc_ss2) and np.array_equal(hc_bg, hc_bg2)
+    return dict(
+        fobs_gw_edges=fobs_gw_edges, fobs_orb_edges=fobs_orb_edges, fobs_orb_cents=fobs_orb_cents,
+        redz_final=redz_final, dnum=dnum, number=number, h2fdf=h2fdf, order=order,
+        hc_ss=hc_ss, hc_bg=hc_bg,
+    )
+
+
+def sam_arrays(sam):
+    dens = sam.static_binary_density
+    out = dict(mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, density=dens,
+               gmt_time=sam._gmt_time, redz_prime=sam._redz_prime)
+    if getattr(sam, "_dens_bef", None) is not None:
+        out["density_noscatter"] = sam._dens_bef
+    return out
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print(f"wrote {path} ({os.path.getsize(path)/1024:.1f} KiB)")
+
+
+def case_small(scatter, tag):
+    shape = (10, 11, 12)
+    sam = make_sam(shape, scatter)
+    base = sam_arrays(sam)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 5)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    res = run_path(sam, hard, fobs_gw_edges, nreals=7, nloud=3, seed=0)
+    save(f"ref_small_2pwl_{tag}.npz", **base, **res, norm=hard._norm, hard_time=3.0 * GYR,
+         sepa_init=hard._sepa_init, rchar=hard._rchar, gamma_inner=hard._gamma_inner,
+         gamma_outer=hard._gamma_outer, num_steps=hard._num_steps, nreals=7, nloud=3, seed=0)
+    res = run_path(sam, holo.hardening.Hard_GW(), fobs_gw_edges, nreals=7, nloud=3, seed=1)
+    save(f"ref_small_gw_{tag}.npz", **base, **res, nreals=7, nloud=3, seed=1)
+
+
+def case_cfg1():
+    """The reference's CPU-runnable workload: shape 30, 20 frequencies, 100 realizations, 5 loudest."""
+    sam = make_sam(30, 0.28)
+    base = sam_arrays(sam)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 20)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    res = run_path(sam, hard, fobs_gw_edges, nreals=100, nloud=5, seed=0)
+    number, h2fdf = res["number"], res["h2fdf"]
+    keep = dict(
+        fobs_gw_edges=res["fobs_gw_edges"], hc_ss=res["hc_ss"], hc_bg=res["hc_bg"],
+        # size-independent summaries of the large grids
+        number_sum_f=number.sum(axis=(0, 1, 2)), mean_hc2_f=(number * h2fdf).sum(axis=(0, 1, 2)),
+        dnum_sum_f=res["dnum"].sum(axis=(0, 1, 2)), redz_final_slice=res["redz_final"][::7, ::7, ::7, :],
+        dnum_slice=res["dnum"][::7, ::7, ::7, :], order_head=res["order"][:2000],
+    )
+    save("ref_cfg1.npz", **base, **keep, norm=hard._norm, nreals=100, nloud=5, seed=0)
+
+
+def case_scatter_shapes():
+    """Density with M-Mbulge scatter on two non-cubic grids (sam.py:1291-1394)."""
+    out = {}
+    for ii, shape in enumerate([(14, 13, 6), (25, 17, 5)]):
+        sam = make_sam(shape, 0.28 if ii == 0 else 0.6)
+        arr = sam_arrays(sam)
+        for kk, vv in arr.items():
+            out[f"s{ii}_{kk}"] = vv
+    save("ref_scatter.npz", **out)
+
+
+def case_norm_sweep():
+    """Hardening normalisations over the library parameter box (sam_cyutils.pyx:289-398)."""
+    sam = make_sam((12, 9, 3), 0.0)
+    mt, mr = [mm.flatten() for mm in np.meshgrid(sam.mtot, sam.mrat, indexing="ij")]
+    rows = []
+    for time_gyr, gin, gout, rchar_pc, sepa_pc, nsteps in [
+        (3.0, -1.0, 2.5, 100.0, 1e3, 300), (0.1, -1.5, 2.5, 100.0, 1e3, 300), (11.0, 0.0, 2.5, 100.0, 1e4, 300),
+        (1.0, -0.5, 1.5, 10.0, 1e3, 100), (6.0, -1.2, 2.5, 100.0, 1e4, 300),
+    ]:
+        nl = sam_cyutils.find_2pwl_hardening_norm(time_gyr * GYR, mt, mr, sepa_pc * PC, rchar_pc * PC, gin, gout, nsteps)
+        rows.append(dict(time=time_gyr * GYR, gamma_inner=gin, gamma_outer=gout, rchar=rchar_pc * PC,
+                         sepa_init=sepa_pc * PC, nsteps=nsteps, norm_log10=np.asarray(nl)))
+    out = dict(mtot=mt, mrat=mr)
+    for ii, row in enumerate(rows):
+        for kk, vv in row.items():
+            out[f"p{ii}_{kk}"] = vv
+    save("ref_norm_sweep.npz", **out, nparams=len(rows))
+
+
+def case_loudest_edges():
+    """``loudest_hc_from_sorted`` edge cases: zero bins, ties, huge expectation (Normal branch), L > sources."""
+    rng = np.random.default_rng(7)
+    shape = (4, 3, 5, 3)
+    number = rng.lognormal(-1.0, 2.0, size=shape)
+    number[0, 0, :, :] = 0.0
+    number[1, 2, 3, :] = 3.0e10       # above the 1e10 Normal threshold
+    number[2, 1, 1, 1] = 5.0e9        # large Poisson (PTRS branch)
+    h2fdf = rng.lognormal(-60.0, 3.0, size=shape)
+    h2fdf[3, :, :, 0] = h2fdf[3, 0, 0, 0]   # ties in the sort key
+    h2fdf[0, 1, 2, :] = 0.0
+    order = np.argsort(-h2fdf[..., 0].flatten())
+    ms, qs, zs = np.unravel_index(order, shape[:3])
+    out = dict(number=number, h2fdf=h2fdf, order=order)
+    for ii, (nreals, nloud, seed) in enumerate([(5, 4, 3), (3, 40, 4), (1, 1, 5)]):
+        seed_rng(seed)
+        ss, bg = cyutils.loudest_hc_from_sorted(number, h2fdf, nreals, nloud, ms, qs, zs)
+        out.update({f"c{ii}_nreals": nreals, f"c{ii}_nloud": nloud, f"c{ii}_seed": seed,
+                    f"c{ii}_hc2ss": ss, f"c{ii}_hc2bg": bg})
+    # second-pass GWB (gravwaves.py:518-522 -> cyutils.pyx:854-897)
+    seed_rng(11)
+    out["gwb_nreals"] = 6
+    out["gwb_seed"] = 11
+    out["gwb_hc2"] = np.asarray(cyutils.sam_poisson_gwb(number, h2fdf, 6))
+    save("ref_loudest_edges.npz", **out, ncases=3)
+
+
+def case_known_answers():
+    """Known-answer values the reference pins for the strain formula (holodeck/tests/test_utils.py:52-96)."""
+    path = os.path.join(ref_env.REF_SRC, "holodeck", "tests", "test_utils.py")
+    tree = ast.parse(open(path).read())
+    vals = {}
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == "test_with_fixed_values":
+            for stmt in node.body:
+                if isinstance(stmt, ast.Assign) and isinstance(stmt.value, ast.List):
+                    try:
+                        vals[stmt.targets[0].id] = np.array(ast.literal_eval(stmt.value), dtype=float)
+                    except (ValueError, TypeError):
+                        pass
+    assert {"m1", "m2", "dc", "mc", "hs"} <= set(vals)
+    freq = 1.0 / YR
+    save("ref_known_answers.npz", m1=vals["m1"], m2=vals["m2"], dc=vals["dc"], mc=vals["mc"], hs=vals["hs"],
+         freq=freq, check_mc=holo.utils.chirp_mass(vals["m1"], vals["m2"]),
+         check_hs=holo.utils.gw_strain_source(vals["mc"], vals["dc"], freq))
+
+
+def main():
+    case_known_answers()
+    case_loudest_edges()
+    case_norm_sweep()
+    case_small(0.0, "noscatter")
+    case_small(0.28, "scatter")
+    case_scatter_shapes()
+    case_cfg1()
+
+
+if __name__ == "__main__":
+    main()
