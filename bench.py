@@ -1,0 +1,356 @@
+"""Benchmark: SAM GWB realizations/s on one GB300 (plain GPU SAM).
+
+Workload (the default-grid configuration): Semi_Analytic_Model on the 91 (mtot) x 81 (mrat) x 101 (redz)
+grid with GSMF_Schechter(phi0=-2.77, mchar0_log10=11.24, alpha0=-1.24), GPF_Power_Law, GMT_Power_Law and
+MMBulge_KH2013(mamp_log10=8.69, mplaw=1.17, scatter 0.28 dex); Fixed_Time_2PL_SAM(3 Gyr, rchar=100 pc,
+gamma_inner=-1, gamma_outer=+2.5, sepa_init=1 kpc); 40 harmonics of 1/(16 yr); 1000 realizations,
+10 loudest.  One step = one full model evaluation: build the SAM (density with M-Mbulge scatter),
+find the hardening normalisation, and gwb() (dynamic binary number, integration, strain, sort,
+Poisson realizations with the loudest split).  value = realizations / s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference path (the oracle) on the host cores.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (91, 81, 101)
+NFREQ = 40
+NREALS = 1000
+NLOUD = 10
+METRIC = "SAM GWB realizations/s on 1 GB300: plain vs batched vs emulator at stated hc error"
+UNIT = "realizations/s"
+CONFIG_NAME = "plain SAM, 91x81x101 grid, 40 harmonics of 1/(16 yr), 1000 realizations, 10 loudest"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+
+def make_model(H, C):
+    gsmf = H.sams.GSMF_Schechter(phi0=-2.77, mchar0_log10=11.24, alpha0=-1.24)
+    mmb = H.host_relations.MMBulge_KH2013(mamp_log10=8.69, mplaw=1.17, scatter_dex=0.28)
+    sam = H.sams.Semi_Analytic_Model(gsmf=gsmf, gpf=H.sams.GPF_Power_Law(), gmt=H.sams.GMT_Power_Law(),
+                                     mmbulge=mmb, shape=SHAPE)
+    hard = H.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * C.GYR, sepa_init=1.0e3 * C.PC, rchar=100.0 * C.PC,
+                                          gamma_inner=-1.0, gamma_outer=2.5)
+    return sam, hard
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def kernel_event_timer(torch):
+    """Times the realization kernel on its launching stream with CUDA events (torch's current stream)."""
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    from holodeck_gb300 import _native as N
+    from holodeck_gb300 import single_sources
+
+    _, fe = H.utils.pta_freqs(16.0 * C.YR, NFREQ)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")   # > 129 MB of L2
+    seed0 = 1000 * (rank + 1)
+    N.reset_launch_count()
+
+    def step(i, keep_on_device=True):
+        sam, hard = make_model(H, C)
+        if keep_on_device:
+            return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i, return_torch=True)
+        return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+
+    # ---- value: device-resident results, K steps between events
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    N.reset_launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for i in range(args.steps):
+        flush.zero_()
+        step(args.warmup + i)
+    t1.record()
+    barrier()
+    launches = N.launch_count()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * NREALS / (ms / 1e3)
+
+    # ---- e2e: the public numpy API (results copied to host every step)
+    barrier()
+    te0 = time.perf_counter()
+    for i in range(args.steps):
+        hc_ss, hc_bg = step(args.warmup + args.steps + i, keep_on_device=False)
+    barrier()
+    e2e_ms = (time.perf_counter() - te0) * 1e3 / args.steps
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    h2d = 8 * (sum(SHAPE) + NFREQ + 1)
+    d2h = int(hc_ss.nbytes + hc_bg.nbytes)
+
+    # ---- roofline of the realization kernel (CUDA events on the launching stream)
+    sam, hard = make_model(H, C)
+    fo_c = H.utils.midpoints(fe) / 2.0
+    rf, dn = sam._dbn_device(hard, fo_c)
+    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf)
+    order = single_sources.sort_order_device(h2fdf)
+    from holodeck_gb300 import cyutils
+    nb = int(number.numel() // NFREQ)
+    times = []
+    for i in range(3):
+        flush.zero_()
+        e0, e1 = kernel_event_timer(torch)
+        e0.record()
+        cyutils.loudest_device(number.reshape(-1, NFREQ), h2fdf.reshape(-1, NFREQ), NREALS, NLOUD, order, seed=i)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t_real = min(times)
+    draws = nb * NFREQ * NREALS
+    # algorithmic bytes of one launch: read number + h2fdf (gathered once), write hc2ss + hc2bg
+    alg_bytes = 2 * 8 * nb * NFREQ * 2 + 8 * NFREQ * NREALS * (NLOUD + 1)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / t_real / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            traffic = json.load(fh).get("k_loudest_philox_bytes_per_launch")
+    except (OSError, ValueError):
+        pass
+
+    cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 grids / f32+int32 realizations",
+            "data": "synthetic (analytic model parameters; no dataset)",
+            "config": {"workload": CONFIG_NAME, "grid": list(SHAPE), "nfreqs": NFREQ, "nreals": NREALS,
+                       "nloudest": NLOUD, "rng": "philox4x32-10", "l2": "flushed (256 MB write) before every step",
+                       "parallelism": f"replicas x{world}",
+                       "note": "scatter geometry plan cached per grid; every other stage recomputed each step"},
+            "e2e": {"value": world * NREALS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"kernel": "k_loudest_philox", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                         "launch_s": t_real, "draws_per_s": draws / t_real,
+                         "note": "issue-bound sampler: HBM fraction shown for the contract, see profiles/"},
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU restatement (oracle): bounded sample, extrapolated to the full workload
+# ------------------------------------------------------------------------------------------------
+
+SAMPLE_Z = 11
+SAMPLE_R = 3
+
+
+def _oracle_sample(seed, nreals):
+    """Times the oracle path on the sample grid (91 x 81 x 11): stage seconds."""
+    from oracle import sam_oracle as O
+    from holodeck_gb300 import constants as C
+    shape = (SHAPE[0], SHAPE[1], SAMPLE_Z)
+    mtot, mrat, redz = O.grid_edges(shape)
+    p = O.default_params(scatter_dex=0.28)
+    t = {}
+    t0 = time.perf_counter()
+    parts = O.static_binary_density(mtot, mrat, redz, p, return_parts=True)
+    t["density"] = time.perf_counter() - t0
+    mt, mr = np.meshgrid(mtot, mrat, indexing="ij")
+    t0 = time.perf_counter()
+    norm = 10.0 ** O.find_2pwl_hardening_norm(3.0 * C.GYR, mt.ravel(), mr.ravel(), 1.0e3 * C.PC, 100.0 * C.PC,
+                                              -1.0, 2.5, 300).reshape(mt.shape)
+    t["norm"] = time.perf_counter() - t0
+    _, fe = O.pta_freqs(16.0 * C.YR, NFREQ)
+    fo_c = O.midpoints(fe) / 2.0
+    t0 = time.perf_counter()
+    rf, dn = O.dbn_2pwl(fo_c, 1.0e3 * C.PC, 300, norm, 100.0 * C.PC, -1.0, 2.5, parts["density"], mtot, mrat, redz,
+                        parts["gmt_time"])
+    t["dbn"] = time.perf_counter() - t0
+    edges = [mtot, mrat, redz, fe / 2.0]
+    t0 = time.perf_counter()
+    number = O.integrate_differential_number_3dx1d(edges, dn)
+    h2fdf = O.char_strain_sq_from_bin_edges_redz(edges, rf)
+    order = O.sort_order(h2fdf)
+    t["integrate_strain"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.loudest_hc_from_sorted(number, h2fdf, nreals, NLOUD, order, seed=seed)
+    t["realize"] = time.perf_counter() - t0
+    return t
+
+
+def _extrapolate(t, nreals_sampled):
+    """Full-workload seconds per model: the Z-sliced stages scale with the redshift bins, the
+    hardening normalisation is Z-independent, realizations scale with bins and count."""
+    zscale = (SHAPE[2] - 1) / (SAMPLE_Z - 1)
+    grid = zscale * (t["density"] + t["dbn"] + t["integrate_strain"]) + t["norm"]
+    per_real = zscale * t["realize"] / nreals_sampled
+    return grid + NREALS * per_real, grid, per_real
+
+
+def cpu_baseline_sample(args):
+    t = _oracle_sample(seed=7, nreals=SAMPLE_R)
+    total, grid, per_real = _extrapolate(t, SAMPLE_R)
+    return {"value": NREALS / total, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": (f"oracle on grid 91x81x{SAMPLE_Z} with {SAMPLE_R} realizations, extrapolated linearly in "
+                       f"redshift bins and realizations: grid stages {grid:.1f} s + {per_real:.2f} s/realization "
+                       f"({', '.join(f'{k} {v:.2f}s' for k, v in t.items())})")}
+
+
+def _worker(args):
+    seed, nreals = args
+    return _oracle_sample(seed, nreals)
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement on all host cores (one sample model per worker process)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    ncores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    results = []
+    with ctx.Pool(ncores) as pool:
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_worker, [(1000 * i + k, SAMPLE_R) for k in range(ncores)])
+            wall = time.perf_counter() - t0
+            if i >= args.warmup:
+                results.append((wall, res))
+    # each worker ran the same sample model; the pool finishes ncores samples per wall time
+    per_model = []
+    for wall, res in results:
+        cpu_total = sum(_extrapolate(t, SAMPLE_R)[0] for t in res) / len(res)
+        cpu_sample = sum(sum(t.values()) for t in res) / len(res)
+        per_model.append(cpu_total * (wall / cpu_sample) / ncores)   # wall-clock seconds per full model
+    sec = statistics.median(per_model)
+    value = NREALS / sec
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": CONFIG_NAME, "grid": list(SHAPE), "nfreqs": NFREQ, "nreals": NREALS,
+                       "nloudest": NLOUD},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
+                             "sample": (f"{ncores} processes, each the oracle on grid 91x81x{SAMPLE_Z} with "
+                                        f"{SAMPLE_R} realizations per step, extrapolated linearly to the full "
+                                        "workload")},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,101 @@
+// Shared device helpers for the holodeck_gb300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "holodeck_gb300.h"
+
+// ---- constants hard-coded in holodeck/sams/sam_cyutils.pyx:30-42 (the Cython kernels' set)
+#define HGB_CY_NWTG 6.6742999e-08
+#define HGB_CY_SPLC 29979245800.0
+#define HGB_CY_MPC 3.08567758e+24
+#define HGB_CY_SCHW 1.4852320538237328e-28
+#define HGB_PI 3.14159265358979323846
+
+// ---- astropy CODATA-2018 values used by the Python stages (holodeck/constants.py:23-55)
+#define HGB_NWTG 6.6743e-08
+#define HGB_SPLC 29979245800.0
+
+namespace hgb {
+
+void set_cuda_error(cudaError_t err);
+int check_launch();
+
+__device__ __forceinline__ void flag(int *d_status, int bits) {
+    if (d_status) atomicOr(d_status, bits);
+}
+
+// Derived constants of the Cython kernels (sam_cyutils.pyx:38-42), evaluated once on the host
+// with the host C library in the same operation order as the Cython module initialisation.
+struct CyConst {
+    double c_dadt;   // GW_DADT_SEP_CONST = -64 G^3 / 5 / c^5
+    double kfreq;    // KEPLER_CONST_FREQ = (1/(2 pi)) sqrt(G)
+    double ksepa;    // KEPLER_CONST_SEPA = G^(1/3) / (2 pi)^(2/3)
+    double fourpi;   // FOUR_PI_SPLC_OVER_MPC = 4 pi c / Mpc
+};
+CyConst cy_const();
+
+// sam_cyutils.pyx:46-49
+__device__ __forceinline__ double hard_gw(double c_dadt, double mtot, double mrat, double sepa) {
+    return c_dadt * pow(mtot, 3.0) * mrat / pow(sepa, 3.0) / pow(1.0 + mrat, 2.0);
+}
+
+// sam_cyutils.pyx:240-253: (-norm * (1+x)^(gi-go)) / x^(gi-1) + GW term
+__device__ __forceinline__ double hard_func_2pwl_gw(double c_dadt, double mt, double mr, double sepa, double norm,
+                                                     double rchar, double gi, double go) {
+    double xx = sepa / rchar;
+    double dadt = -norm * pow(1.0 + xx, -go + gi) / pow(xx, gi - 1.0);
+    dadt += hard_gw(c_dadt, mt, mr, sepa);
+    return dadt;
+}
+
+// holodeck/cyutils.pyx:326-358
+__device__ __forceinline__ double interp_between(double xnew, double xl, double xr, double yl, double yr) {
+    return yl + (yr - yl) * (xnew - xl) / (xr - xl);
+}
+
+// sam_cyutils.pyx:66-85, the bracket index of `val` in an increasing table, walking from `start`
+__device__ __forceinline__ int while_while_increasing(int start, int size, double val, const double *edges) {
+    int index = start;
+    while ((index < size - 2) && (edges[index + 1] < val)) index += 1;
+    while ((index > 0) && (edges[index] > val)) index -= 1;
+    return index;
+}
+
+// The index sam_cyutils.pyx:88-107 reaches when walking forward from 0 through a decreasing table:
+// the first i with edges[i+1] <= val, capped at size-1.
+__device__ __forceinline__ int bracket_decreasing_from0(int size, double val, const double *edges) {
+    int lo = 0, hi = size - 1;   // answer in [0, size-1]
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (edges[mid + 1] > val) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Comoving distance [cm] from the Hermite table in u = sqrt(1/(1+z)).
+__device__ __forceinline__ double comoving_distance(const double *dval, const double *dder, int n, double z) {
+    double u = sqrt(1.0 / (1.0 + z));
+    double x = u * (double)n;
+    int k = (int)x;
+    if (k >= n) k = n - 1;
+    if (k < 0) k = 0;
+    double t = x - (double)k;
+    double h = 1.0 / (double)n;
+    double t2 = t * t, t3 = t2 * t;
+    double h00 = 2.0 * t3 - 3.0 * t2 + 1.0;
+    double h10 = t3 - 2.0 * t2 + t;
+    double h01 = -2.0 * t3 + 3.0 * t2;
+    double h11 = t3 - t2;
+    return h00 * dval[k] + h10 * h * dder[k] + h01 * dval[k + 1] + h11 * h * dder[k + 1];
+}
+
+__host__ __device__ __forceinline__ long ceil_div(long a, long b) { return (a + b - 1) / b; }
+
+}  // namespace hgb
+
+#define HGB_CHECK_ARG(cond)                        \
+    do {                                           \
+        if (!(cond)) return HGB_ERR_INVALID_ARGUMENT; \
+    } while (0)

@@ -1,0 +1,461 @@
+// Binary hardening on the GPU:
+//  * hgb_find_2pwl_hardening_norm: Brent root of the two-power-law lifetime per (mtot, mrat) cell
+//    (holodeck/sams/sam_cyutils.pyx:289-398); one warp per cell.
+//  * hgb_dbn_2pwl: differential binary number for Fixed_Time_2PL_SAM (sam_cyutils.pyx:510-781);
+//    one block per (mtot, mrat) cell, one thread per starting redshift, step tables in shared memory.
+//  * hgb_dbn_gw: differential binary number for Hard_GW (sam_cyutils.pyx:788-899); one thread per
+//    grid point.
+// FP64 throughout (the hardening integral and the lookback-time -> redshift inversion are the
+// FP64 islands of the path).  Built with -fmad=false so operation order and rounding follow the
+// reference loops; the remaining differences are the last-ulp behaviour of pow/log10.
+#include <math.h>
+
+#include "hgb_common.cuh"
+
+namespace {
+
+using hgb::CyConst;
+
+constexpr double NORM_LOG10_LO = -20.0;
+constexpr double NORM_LOG10_HI = +20.0;
+constexpr double BRENT_XTOL = 1e-3;
+constexpr double BRENT_RTOL = 1e-5;
+constexpr int BRENT_MAXITER = 100;
+
+// ------------------------------------------------------------------------------------------------
+// hardening normalisation
+// ------------------------------------------------------------------------------------------------
+
+struct NormArgs {
+    double target_time, sepa_init_log10, rchar, gi, go;
+    int nsteps;
+};
+
+// Lifetime minus target for one cell, evaluated by the whole warp (sam_cyutils.pyx:360-398).
+// sepa/aa/bb/gw hold, per separation node, the norm-independent pieces of the hardening rate;
+// the trapezoid terms are formed in parallel and summed in step order by lane 0 so the sum
+// rounds like the reference loop.
+__device__ double warp_lifetime(double norm_log10, const NormArgs &a, const double *sepa, const double *aa,
+                                const double *bb, const double *gw, double *dt, int lane) {
+    double norm = pow(10.0, norm_log10);
+    for (int s = lane; s < a.nsteps; s += 32) {
+        double dl = -norm * aa[s] / bb[s];
+        dl += gw[s];
+        double dr = -norm * aa[s + 1] / bb[s + 1];
+        dr += gw[s + 1];
+        dt[s] = 2.0 * (sepa[s + 1] - sepa[s]) / (dl + dr);
+    }
+    __syncwarp();
+    double time = 0.0;
+    if (lane == 0) {
+        for (int s = 0; s < a.nsteps; s++) time += dt[s];
+    }
+    time = __shfl_sync(0xffffffffu, time, 0);
+    __syncwarp();
+    return time - a.target_time;
+}
+
+// Brent's method (Brent 1973, "Algorithms for Minimization without Derivatives", ch. 4) with the
+// tolerance delta = (xtol + rtol |b|) / 2; returns 0 when the interval does not bracket a root
+// and the last iterate when the iteration budget runs out.  All lanes run it in lock step.
+__device__ double warp_brent(const NormArgs &a, const double *sepa, const double *aa, const double *bb,
+                             const double *gw, double *dt, int lane, int *n_iter_out) {
+    double xa = NORM_LOG10_LO, xb = NORM_LOG10_HI;
+    double fa = warp_lifetime(xa, a, sepa, aa, bb, gw, dt, lane);
+    double fb = warp_lifetime(xb, a, sepa, aa, bb, gw, dt, lane);
+    *n_iter_out = 0;
+    if (fa * fb > 0.0) return 0.0;
+    if (fa == 0.0) return xa;
+    if (fb == 0.0) return xb;
+    double xc = xa, fc = fa;
+    double d = xb - xa, e = d;
+    for (int it = 0; it < BRENT_MAXITER; it++) {
+        *n_iter_out = it + 1;
+        if (fb * fc > 0.0) {
+            xc = xa;
+            fc = fa;
+            d = xb - xa;
+            e = d;
+        }
+        if (fabs(fc) < fabs(fb)) {
+            xa = xb; xb = xc; xc = xa;
+            fa = fb; fb = fc; fc = fa;
+        }
+        double tol = 0.5 * (BRENT_XTOL + BRENT_RTOL * fabs(xb));
+        double m = 0.5 * (xc - xb);
+        if (fb == 0.0 || fabs(m) < tol) return xb;
+        if (fabs(e) > tol && fabs(fb) < fabs(fa)) {
+            double s;
+            if (xa == xc) {
+                s = -fb * (xb - xa) / (fb - fa);                               // secant
+            } else {
+                double da = (fa - fb) / (xa - xb);
+                double dc = (fc - fb) / (xc - xb);
+                s = -fb * (fc * dc - fa * da) / (dc * da * (fc - fa));         // inverse quadratic
+            }
+            if (2.0 * fabs(s) < fmin(fabs(e), 3.0 * fabs(m) - tol)) {
+                e = d;
+                d = s;
+            } else {
+                d = m;
+                e = m;
+            }
+        } else {
+            d = m;
+            e = m;
+        }
+        xa = xb;
+        fa = fb;
+        xb = xb + ((fabs(d) > tol) ? d : ((m > 0.0) ? tol : -tol));
+        fb = warp_lifetime(xb, a, sepa, aa, bb, gw, dt, lane);
+    }
+    *n_iter_out = BRENT_MAXITER + 1;
+    return xb;
+}
+
+__global__ void k_hardening_norm(CyConst cc, NormArgs a, const double *__restrict__ mtot,
+                                 const double *__restrict__ mrat, int n, double *__restrict__ norm_log10,
+                                 double *__restrict__ norm, int *d_status) {
+    extern __shared__ double smem[];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int nwarps = blockDim.x >> 5;
+    int cell = blockIdx.x * nwarps + warp;
+    if (cell >= n) return;   // whole warp exits together
+    int S = a.nsteps;
+    double *sepa = smem + (size_t)warp * 5 * (S + 1);
+    double *aa = sepa + (S + 1);
+    double *bb = aa + (S + 1);
+    double *gw = bb + (S + 1);
+    double *dt = gw + (S + 1);
+    double mt = mtot[cell], mr = mrat[cell];
+
+    // separation nodes: log10 separation stepped down by repeated subtraction (sam_cyutils.pyx:367-383)
+    double risco_log10 = log10(3.0 * HGB_CY_SCHW * mt);
+    double dx = (a.sepa_init_log10 - risco_log10) / S;
+    if (lane == 0) {
+        double sl = a.sepa_init_log10;
+        sepa[0] = sl;
+        for (int s = 1; s <= S; s++) {
+            sl -= dx;
+            sepa[s] = sl;
+        }
+    }
+    __syncwarp();
+    for (int s = lane; s <= S; s += 32) {
+        double sp = pow(10.0, sepa[s]);
+        double xx = sp / a.rchar;
+        aa[s] = pow(1.0 + xx, -a.go + a.gi);
+        bb[s] = pow(xx, a.gi - 1.0);
+        gw[s] = hgb::hard_gw(cc.c_dadt, mt, mr, sp);
+        sepa[s] = sp;
+    }
+    __syncwarp();
+    int nit;
+    double root = warp_brent(a, sepa, aa, bb, gw, dt, lane, &nit);
+    if (lane == 0) {
+        norm_log10[cell] = root;
+        if (norm) norm[cell] = pow(10.0, root);
+        if (nit > BRENT_MAXITER) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// differential binary number, Fixed_Time_2PL_SAM
+// ------------------------------------------------------------------------------------------------
+
+struct Dbn2plArgs {
+    double sepa_init_log10, rchar, gi, go;
+    int num_steps, n_freq, fobs_sorted;
+    int n_mtot, n_mrat, n_redz, n_interp;
+};
+
+__global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ fobs,
+                           const double *__restrict__ hard_norm, const double *__restrict__ nden,
+                           const double *__restrict__ mtot, const double *__restrict__ mrat,
+                           const double *__restrict__ redz, const double *__restrict__ gmt_time,
+                           const double *__restrict__ zgrid_g, const double *__restrict__ agrid_g,
+                           const double *__restrict__ dgrid_g, double *__restrict__ redz_final,
+                           double *__restrict__ diff_num) {
+    extern __shared__ double smem[];
+    const int S = a.num_steps, NI = a.n_interp, NF = a.n_freq;
+    double *zg = smem;
+    double *ag = zg + NI;
+    double *dg = ag + NI;
+    double *ft = dg + NI;
+    double *sepa = ft + NF;          // [S+1]
+    double *frst = sepa + (S + 1);   // [S+1]
+    double *dadt = frst + (S + 1);   // [S+1]
+    double *dts = dadt + (S + 1);    // [S]
+    double *tevo = dts + S;          // [S]
+
+    int cell = blockIdx.x;
+    int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
+    double mt = mtot[ii], mr = mrat[jj];
+    double norm = hard_norm[cell];
+
+    for (int i = threadIdx.x; i < NI; i += blockDim.x) {
+        zg[i] = zgrid_g[i];
+        ag[i] = agrid_g[i];
+        dg[i] = dgrid_g[i];
+    }
+    for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = fobs[i];
+    double risco = 3.0 * HGB_CY_SCHW * mt;
+    double dx = (a.sepa_init_log10 - log10(risco)) / S;
+    if (threadIdx.x == 0) {
+        double sl = a.sepa_init_log10;
+        sepa[0] = sl;
+        for (int s = 1; s <= S; s++) {
+            sl -= dx;
+            sepa[s] = sl;
+        }
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s <= S; s += blockDim.x) {
+        double sp = pow(10.0, sepa[s]);
+        sepa[s] = sp;
+        frst[s] = cc.kfreq * sqrt(mt) / pow(sp, 1.5);
+        dadt[s] = hgb::hard_func_2pwl_gw(cc.c_dadt, mt, mr, sp, norm, a.rchar, a.gi, a.go);
+    }
+    __syncthreads();
+    for (int s = threadIdx.x; s < S; s += blockDim.x) dts[s] = 2.0 * (sepa[s + 1] - sepa[s]) / (dadt[s] + dadt[s + 1]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double te = 0.0;
+        for (int s = 0; s < S; s++) {
+            te += dts[s];
+            tevo[s] = te;
+        }
+    }
+    __syncthreads();
+
+    // Steps that cannot bracket any target are skipped without changing a result: the observed
+    // frequency of a step is at most its rest-frame frequency (z >= 0 after clamping) and at least
+    // frst / (1 + z_start), because the redshift only decreases from the starting redshift.
+    __shared__ double s_fmax;
+    __shared__ int s_first;
+    if (threadIdx.x == 0) {
+        double fmin = ft[0], fmax = ft[0];
+        for (int f = 1; f < NF; f++) {
+            fmin = fmin < ft[f] ? fmin : ft[f];
+            fmax = fmax > ft[f] ? fmax : ft[f];
+        }
+        int first = 0;   // first step whose right edge reaches fmin
+        while (first < S && frst[first + 1] < fmin) first++;
+        s_fmax = fmax;
+        s_first = first;
+    }
+    __syncthreads();
+    const double fmax = s_fmax;
+    const int s_begin = s_first;
+
+    const double age_universe = ag[NI - 1];
+    for (int kk = threadIdx.x; kk < a.n_redz; kk += blockDim.x) {
+        long row = ((long)cell * a.n_redz + kk);
+        double *rf = redz_final + row * NF;
+        double *dn = diff_num + row * NF;
+        for (int f = 0; f < NF; f++) {
+            rf[f] = -1.0;
+            dn[f] = 0.0;
+        }
+        // age at the starting redshift (sam_cyutils.pyx:563-573)
+        double zk = redz[kk];
+        int zi = hgb::bracket_decreasing_from0(NI, zk, zg);
+        if (zi > NI - 2) zi = NI - 2;
+        double rage = hgb::interp_between(zk, zg[zi], zg[zi + 1], ag[zi], ag[zi + 1]);
+        double gmt = gmt_time[row];
+        double nd = nden[row];
+        const double fstop = fmax * (1.0 + zk) * (1.0 + 1e-12);
+        int il = 0;
+        int fp = 0;                 // first target >= the left frequency (targets ascending)
+        bool have_prev = false;     // right edge of the previous step, reused as this step's left edge
+        double prev_tr = 0.0, prev_zr = 0.0, prev_fr = 0.0;
+        for (int s = s_begin; s < S; s++) {
+            if (frst[s] > fstop) break;
+            double time_right = tevo[s] + gmt + rage;
+            double time_left, redz_left, fl;
+            bool reuse = have_prev;
+            have_prev = false;
+            if (reuse) {
+                time_left = prev_tr;
+            } else {
+                time_left = time_right - dts[s];
+            }
+            if (time_left > age_universe) continue;
+            if (reuse) {
+                redz_left = prev_zr;
+            } else {
+                il = hgb::while_while_increasing(il, NI, time_left, ag);
+                redz_left = hgb::interp_between(time_left, ag[il], ag[il + 1], zg[il], zg[il + 1]);
+            }
+            if (redz_left < 0.0) continue;
+            fl = reuse ? prev_fr : frst[s] / (1.0 + redz_left);
+            int ir = hgb::while_while_increasing(il, NI, time_right, ag);
+            double redz_right = hgb::interp_between(time_right, ag[ir], ag[ir + 1], zg[ir], zg[ir + 1]);
+            double zr_raw = redz_right;
+            if (redz_right < 0.0) redz_right = 0.0;
+            double fr = frst[s + 1] / (1.0 + redz_right);
+            if (zr_raw >= 0.0) {
+                have_prev = true;
+                prev_tr = time_right;
+                prev_zr = zr_raw;
+                prev_fr = fr;
+            }
+            int il_step = il;
+            il = ir;
+            int f0;
+            if (a.fobs_sorted) {
+                while (fp > 0 && ft[fp - 1] >= fl) fp--;
+                while (fp < NF && ft[fp] < fl) fp++;
+                f0 = fp;
+                if (f0 >= NF || ft[f0] > fr) continue;
+            } else {
+                f0 = 0;
+            }
+            for (int f = f0; f < NF; f++) {
+                double ftarget = ft[f];
+                if (ftarget < fl || fr < ftarget) {
+                    if (a.fobs_sorted) break;   // ascending targets: nothing further lies inside
+                    continue;
+                }
+                double new_time = hgb::interp_between(ftarget, fl, fr, time_left, time_right);
+                if (new_time > ag[NI - 1]) break;
+                int ni = hgb::while_while_increasing(il_step, NI, new_time, ag);
+                double new_redz = hgb::interp_between(new_time, ag[ni], ag[ni + 1], zg[ni], zg[ni + 1]);
+                double dcom = hgb::interp_between(new_time, ag[ni], ag[ni + 1], dg[ni], dg[ni + 1]);
+                rf[f] = new_redz;
+                double target_frst_orb = ftarget * (1.0 + new_redz);
+                double sp = cc.ksepa * pow(mt, 1.0 / 3.0) / pow(target_frst_orb, 2.0 / 3.0);
+                double dadt_t = hgb::hard_func_2pwl_gw(cc.c_dadt, mt, mr, sp, norm, a.rchar, a.gi, a.go);
+                double tres = -(2.0 / 3.0) * sp / dadt_t;
+                double dcm = dcom / HGB_CY_MPC;
+                double cosmo_fact = cc.fourpi * (1.0 + new_redz) * (dcm * dcm);
+                dn[f] = nd * tres * cosmo_fact;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// differential binary number, Hard_GW
+// ------------------------------------------------------------------------------------------------
+
+__global__ void k_dbn_gw(CyConst cc, const double *__restrict__ fobs, int NF, const double *__restrict__ nden,
+                         const double *__restrict__ mtot, int nm, const double *__restrict__ mrat, int nq, int nz,
+                         const double *__restrict__ redz_prime, const double *__restrict__ zgrid,
+                         const double *__restrict__ dgrid, int NI, double *__restrict__ redz_final,
+                         double *__restrict__ diff_num) {
+    long row = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= (long)nm * nq * nz) return;
+    int jj = (int)((row / nz) % nq);
+    int ii = (int)(row / ((long)nz * nq));
+    double *rf = redz_final + row * NF;
+    double *dn = diff_num + row * NF;
+    for (int f = 0; f < NF; f++) {
+        rf[f] = -1.0;
+        dn[f] = 0.0;
+    }
+    double rzp = redz_prime[row];
+    if (rzp <= 0.0) return;
+    double mt = mtot[ii], mr = mrat[jj];
+    double rad_isco = 3.0 * HGB_CY_SCHW * mt;
+    double frst_orb_isco = cc.kfreq * sqrt(mt) / pow(rad_isco, 1.5);
+    int zi = hgb::bracket_decreasing_from0(NI, rzp, zgrid);
+    if (zi > NI - 2) zi = NI - 2;
+    double dcom = hgb::interp_between(rzp, zgrid[zi], zgrid[zi + 1], dgrid[zi], dgrid[zi + 1]);
+    double nd = nden[row];
+    for (int f = 0; f < NF; f++) {
+        rf[f] = rzp;
+        double target_frst_orb = fobs[f] * (1.0 + rzp);
+        if (target_frst_orb > frst_orb_isco) {
+            for (int fp = f + 1; fp < NF; fp++) rf[fp] = rzp;
+            break;
+        }
+        double sp = cc.ksepa * pow(mt, 1.0 / 3.0) / pow(target_frst_orb, 2.0 / 3.0);
+        double dadt = hgb::hard_gw(cc.c_dadt, mt, mr, sp);
+        double tres = -(2.0 / 3.0) * sp / dadt;
+        double dcm = dcom / HGB_CY_MPC;
+        double cosmo_fact = cc.fourpi * (1.0 + rzp) * (dcm * dcm);
+        dn[f] = nd * tres * cosmo_fact;
+    }
+}
+
+size_t norm_smem_per_warp(int nsteps) { return (size_t)5 * (nsteps + 1) * sizeof(double); }
+
+}  // namespace
+
+extern "C" {
+
+int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const double *mrat, int n,
+                                 double sepa_init, double rchar, double gamma_inner, double gamma_outer,
+                                 int nsteps, double *norm_log10, double *norm, int *d_status, void *stream) {
+    HGB_CHECK_ARG(mtot && mrat && norm_log10 && n >= 0);
+    HGB_CHECK_ARG(nsteps > 0 && sepa_init > 0.0 && rchar > 0.0);
+    size_t per_warp = norm_smem_per_warp(nsteps);
+    HGB_CHECK_ARG(per_warp <= 200 * 1024);
+    if (n == 0) return HGB_OK;
+    int wpb = (int)(48 * 1024 / per_warp);
+    if (wpb > 4) wpb = 4;
+    if (wpb < 1) wpb = 1;
+    size_t smem = per_warp * wpb;
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(k_hardening_norm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+    }
+    NormArgs a{target_time, log10(sepa_init), rchar, gamma_inner, gamma_outer, nsteps};
+    unsigned blocks = (unsigned)hgb::ceil_div(n, wpb);
+    k_hardening_norm<<<blocks, 32 * wpb, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, mtot, mrat, n,
+                                                                       norm_log10, norm, d_status);
+    return hgb::check_launch();
+}
+
+int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                 const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                 const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                 const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                 double *redz_final, double *diff_num, void *stream) {
+    HGB_CHECK_ARG(fobs_orb && hard_norm && nden && mtot && mrat && redz && gmt_time && cosmo);
+    HGB_CHECK_ARG(redz_final && diff_num);
+    HGB_CHECK_ARG(n_freq > 0 && num_steps > 0 && n_mtot > 0 && n_mrat > 0 && n_redz > 0);
+    HGB_CHECK_ARG(cosmo->grid_size >= 2 && cosmo->grid_z && cosmo->grid_age && cosmo->grid_dcom);
+    HGB_CHECK_ARG(sepa_init > 0.0 && rchar > 0.0);
+    Dbn2plArgs a{log10(sepa_init), rchar, gamma_inner, gamma_outer, num_steps, n_freq, fobs_sorted ? 1 : 0,
+                 n_mtot, n_mrat, n_redz, cosmo->grid_size};
+    size_t smem = sizeof(double) * ((size_t)3 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
+                                    2 * (size_t)num_steps);
+    HGB_CHECK_ARG(smem <= 200 * 1024);
+    if (smem > 48 * 1024) {
+        cudaError_t err = cudaFuncSetAttribute(k_dbn_2pwl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+    }
+    int threads = ((n_redz + 31) / 32) * 32;
+    if (threads > 256) threads = 256;
+    unsigned blocks = (unsigned)((long)n_mtot * n_mrat);
+    k_dbn_2pwl<<<blocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden, mtot,
+                                                                mrat, redz, gmt_time, cosmo->grid_z,
+                                                                cosmo->grid_age, cosmo->grid_dcom, redz_final,
+                                                                diff_num);
+    return hgb::check_launch();
+}
+
+int hgb_dbn_gw(const double *fobs_orb, int n_freq, const double *nden, const double *mtot, int n_mtot,
+               const double *mrat, int n_mrat, int n_redz, const double *redz_prime, const hgb_cosmo *cosmo,
+               double *redz_final, double *diff_num, void *stream) {
+    HGB_CHECK_ARG(fobs_orb && nden && mtot && mrat && redz_prime && cosmo && redz_final && diff_num);
+    HGB_CHECK_ARG(n_freq > 0 && n_mtot > 0 && n_mrat > 0 && n_redz > 0);
+    HGB_CHECK_ARG(cosmo->grid_size >= 2 && cosmo->grid_z && cosmo->grid_dcom);
+    long n = (long)n_mtot * n_mrat * n_redz;
+    int threads = 128;
+    k_dbn_gw<<<(unsigned)hgb::ceil_div(n, threads), threads, 0, (cudaStream_t)stream>>>(
+        hgb::cy_const(), fobs_orb, n_freq, nden, mtot, n_mtot, mrat, n_mrat, n_redz, redz_prime, cosmo->grid_z,
+        cosmo->grid_dcom, cosmo->grid_size, redz_final, diff_num);
+    return hgb::check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+// Cell integration and per-bin strain on the (M-1, Q-1, Z-1, F) bin grid (kernel k_cells):
+//  * NUMBER: integrate_differential_number_3dx1d (holodeck/sams/sam_cyutils.pyx:115-216)
+//  * STRAIN: char_strain_sq_from_bin_edges_redz (holodeck/gravwaves.py:694-724)
+//  * both in one pass for gwb() (sam.py:930-935): each vertex of dnum and redz_final is read from
+//    L1/L2 by the eight bins that share it, and number / h2fdf are written once.
+// One block per (mtot, mrat) cell; its threads walk the (redz, frequency) elements with the
+// frequency fastest, so the eight vertex loads of a warp are contiguous runs along the frequency
+// axis.  Built with -fmad=false: the eight-vertex sum and the midpoints round like the Cython/numpy
+// code; the strain product is regrouped (see cell_strain), which moves it by a few ulp.
+#include <math.h>
+
+#include "hgb_common.cuh"
+
+namespace {
+
+struct BinGeom {
+    int nm, nq, nz, nf;   // edge counts of mtot, mrat, redz; number of frequencies
+};
+
+__device__ __forceinline__ long vtx(const BinGeom &g, int m, int q, int z, int f) {
+    return (((long)m * g.nq + q) * g.nz + z) * g.nf + f;
+}
+
+// sam_cyutils.pyx:199-214
+__device__ __forceinline__ double cell_number(const BinGeom &g, const double *dnum, int m, int q, int z, int f,
+                                              const double *log10_mtot, const double *mrat, const double *redz,
+                                              const double *dln_freq) {
+    double dm = log10_mtot[m + 1] - log10_mtot[m];
+    double dmdq = dm * (mrat[q + 1] - mrat[q]);
+    double dmdqdz = dmdq * (redz[z + 1] - redz[z]);
+    double temp = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++) temp += dnum[vtx(g, m + ii, q + jj, z + kk, f)];
+    return temp * dmdqdz * dln_freq[f] / 8.0;
+}
+
+struct StrainArgs {
+    double gw_src_const;
+    const double *dc_val, *dc_der;
+    int dc_n;
+};
+
+// gravwaves.py:694-724 rearranged: hs = K mc (2 mc fr)^(2/3) / dc with fr = fc (1 + zbar) is evaluated
+// as [K mc (2 mc)^(2/3)] [fc^(2/3)] [(1 + zbar)^(2/3)] / dc, the first factor once per (mtot, mrat)
+// cell and the second once per frequency, so each (bin, frequency) costs one cube root and the
+// comoving-distance lookup.  The redshift midpoints are taken along mtot, then mrat, then redz.
+__device__ __forceinline__ double cell_strain(const BinGeom &g, const double *rz, int m, int q, int z, int f,
+                                              double amp_mq, double amp_f, double fc_df, const StrainArgs &s,
+                                              int *d_status) {
+    double r[2][2][2];
+#pragma unroll
+    for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++) {
+                double v = rz[vtx(g, m + ii, q + jj, z + kk, f)];
+                if (v < 0.0 && v != -1.0) hgb::flag(d_status, HGB_STATUS_INVALID_REDSHIFT);
+                r[ii][jj][kk] = v;
+            }
+    double a00 = 0.5 * (r[1][0][0] + r[0][0][0]);
+    double a01 = 0.5 * (r[1][0][1] + r[0][0][1]);
+    double a10 = 0.5 * (r[1][1][0] + r[0][1][0]);
+    double a11 = 0.5 * (r[1][1][1] + r[0][1][1]);
+    double b0 = 0.5 * (a10 + a00);
+    double b1 = 0.5 * (a11 + a01);
+    double zb = 0.5 * (b1 + b0);
+    if (!(zb > 0.0)) return 0.0;   // +inf comoving distance: zero strain
+    double dc = hgb::comoving_distance(s.dc_val, s.dc_der, s.dc_n, zb);
+    double zp1 = 1.0 + zb;
+    double hs = amp_mq * amp_f * cbrt(zp1 * zp1) / dc;
+    return (hs * hs) * fc_df;
+}
+
+// One block per (mtot, mrat) bin cell; threads stride over its (redz, frequency) elements.
+template <bool NUMBER, bool STRAIN>
+__global__ void k_cells(BinGeom g, StrainArgs s, const double *__restrict__ mtot, const double *__restrict__ log10_mtot,
+                        const double *__restrict__ mrat, const double *__restrict__ redz,
+                        const double *__restrict__ fedges, const double *__restrict__ dln_freq,
+                        const double *__restrict__ dnum, const double *__restrict__ redz_final,
+                        double *__restrict__ number, double *__restrict__ h2fdf, int *d_status) {
+    extern __shared__ double sm[];
+    double *amp_f = sm;              // [nf] fc^(2/3)
+    double *fc_df = sm + g.nf;       // [nf] fc / df
+    __shared__ double amp_mq;
+    const int cell = blockIdx.x;
+    const int m = cell / (g.nq - 1), q = cell % (g.nq - 1);
+    if (STRAIN) {
+        for (int f = threadIdx.x; f < g.nf; f += blockDim.x) {
+            double fc = 0.5 * (fedges[f + 1] + fedges[f]);
+            double df = fedges[f + 1] - fedges[f];
+            amp_f[f] = pow(fc, 2.0 / 3.0);
+            fc_df[f] = fc / df;
+        }
+        if (threadIdx.x == 0) {
+            double mt = 0.5 * (mtot[m + 1] + mtot[m]);
+            double mr = 0.5 * (mrat[q + 1] + mrat[q]);
+            double mc = mt * pow(mr, 3.0 / 5.0) / pow(1.0 + mr, 6.0 / 5.0);
+            amp_mq = s.gw_src_const * mc * pow(2.0 * mc, 2.0 / 3.0);
+        }
+        __syncthreads();
+    }
+    const int nzf = (g.nz - 1) * g.nf;
+    const long out0 = (long)cell * nzf;
+    for (int e = threadIdx.x; e < nzf; e += blockDim.x) {
+        int z = e / g.nf, f = e % g.nf;
+        if (NUMBER) number[out0 + e] = cell_number(g, dnum, m, q, z, f, log10_mtot, mrat, redz, dln_freq);
+        if (STRAIN) h2fdf[out0 + e] = cell_strain(g, redz_final, m, q, z, f, amp_mq, amp_f[f], fc_df[f], s, d_status);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hgb_integrate_3dx1d(const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat, const double *redz,
+                        int n_redz, const double *dln_freq, int n_freq, const double *dnum, double *number,
+                        void *stream) {
+    HGB_CHECK_ARG(log10_mtot && mrat && redz && dln_freq && dnum && number);
+    HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
+    BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
+    StrainArgs s{0.0, nullptr, nullptr, 0};
+    unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
+    k_cells<true, false><<<cells, 256, 0, (cudaStream_t)stream>>>(g, s, nullptr, log10_mtot, mrat, redz, nullptr,
+                                                                  dln_freq, dnum, nullptr, number, nullptr, nullptr);
+    return hgb::check_launch();
+}
+
+int hgb_char_strain_sq(const double *mtot, int n_mtot, const double *mrat, int n_mrat, int n_redz,
+                       const double *fobs_orb_edges, int n_freq, const double *redz_final, double gw_src_const,
+                       const hgb_cosmo *cosmo, double *h2fdf, int *d_status, void *stream) {
+    HGB_CHECK_ARG(mtot && mrat && fobs_orb_edges && redz_final && cosmo && h2fdf);
+    HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
+    HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
+    BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
+    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
+    size_t smem = sizeof(double) * 2 * n_freq;
+    HGB_CHECK_ARG(smem <= 48 * 1024);
+    k_cells<false, true><<<cells, 256, smem, (cudaStream_t)stream>>>(g, s, mtot, nullptr, mrat, nullptr, fobs_orb_edges,
+                                                                     nullptr, nullptr, redz_final, nullptr, h2fdf,
+                                                                     d_status);
+    return hgb::check_launch();
+}
+
+int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat,
+                          const double *redz, int n_redz, const double *fobs_orb_edges, const double *dln_freq,
+                          int n_freq, const double *dnum, const double *redz_final, double gw_src_const,
+                          const hgb_cosmo *cosmo, double *number, double *h2fdf, int *d_status, void *stream) {
+    HGB_CHECK_ARG(mtot && log10_mtot && mrat && redz && fobs_orb_edges && dln_freq && dnum && redz_final);
+    HGB_CHECK_ARG(cosmo && number && h2fdf);
+    HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
+    HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
+    BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
+    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
+    size_t smem = sizeof(double) * 2 * n_freq;
+    HGB_CHECK_ARG(smem <= 48 * 1024);
+    k_cells<true, true><<<cells, 256, smem, (cudaStream_t)stream>>>(g, s, mtot, log10_mtot, mrat, redz, fobs_orb_edges,
+                                                                    dln_freq, dnum, redz_final, number, h2fdf, d_status);
+    return hgb::check_launch();
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+"""GPU versions of the holodeck/cyutils.pyx functions on the SAM path.
+
+``loudest_hc_from_sorted`` (cyutils.pyx:1220-1264) and ``sam_poisson_gwb`` (cyutils.pyx:854-897)
+keep the reference's argument lists.  Two keyword arguments are added:
+
+* ``seed``   -- 64-bit key of the Philox draws (default: fresh entropy, like the reference's
+               unseeded ``PCG64()``);
+* ``replay`` -- the draws themselves, to reproduce a numpy PCG64 stream bit for bit:
+               (R, F, B) in the sorted-bin order for ``loudest_hc_from_sorted`` and (B, F, R)
+               for ``sam_poisson_gwb`` (the reference's draw order in both cases).
+"""
+
+import os
+
+import numpy as np
+
+from . import _device as D
+from . import _native as N
+
+NORMAL_THRESHOLD = 1e10
+
+
+def new_seed():
+    return int.from_bytes(os.urandom(8), "little")
+
+
+def _check_threshold(normal_threshold):
+    if int(normal_threshold) != int(NORMAL_THRESHOLD):
+        raise ValueError(f"normal_threshold={normal_threshold}: only the reference default 1e10 is supported")
+
+
+def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=None, status=None):
+    """Device (hc2ss[F, R, L], hc2bg[F, R]) from device number/h2fdf (B, F) and order (B,) int32."""
+    t = D.torch()
+    nf = int(number.shape[-1])
+    nb = int(number.numel() // nf)
+    dev = number.device
+    hc2ss = t.empty((nf, nreals, nloudest), dtype=t.float64, device=dev)
+    hc2bg = t.empty((nf, nreals), dtype=t.float64, device=dev)
+    mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
+    rep = None
+    if replay is not None:
+        rep = D.as_device(replay)
+        if tuple(rep.shape) != (nreals, nf, nb):
+            raise ValueError(f"replay must be shaped (R, F, B)=({nreals}, {nf}, {nb}), got {tuple(rep.shape)}")
+    lib = N.load()
+    ws_bytes = lib.hgb_loudest_workspace_bytes(nb, nf, int(nreals), int(nloudest), mode)
+    ws = D.workspace(ws_bytes, dev)
+    st = status if status is not None else D.StatusWord(dev)
+    seed = new_seed() if seed is None else int(seed) & 0xFFFFFFFFFFFFFFFF
+    N.call("hgb_loudest_hc_from_sorted", N.ptr(number), N.ptr(h2fdf), nb, nf, int(nreals), int(nloudest),
+           N.ptr(order), mode, seed, N.ptr(rep), N.ptr(hc2ss), N.ptr(hc2bg), N.ptr(ws), int(ws_bytes), st.ptr,
+           N.stream_handle())
+    return hc2ss, hc2bg
+
+
+def loudest_hc_from_sorted(number, h2fdf, nreals, nloudest, msort, qsort, zsort, normal_threshold=1e10,
+                           seed=None, replay=None):
+    """hc^2 of the loudest sources (F, R, L) and of the background (F, R); cyutils.pyx:1220-1264."""
+    _check_threshold(normal_threshold)
+    like_torch = D.is_torch(number)
+    shape = tuple(number.shape)
+    num = D.as_device(number).reshape(-1, shape[-1])
+    hh = D.as_device(h2fdf).reshape(-1, shape[-1])
+    ms, qs, zs = [np.asarray(D.to_host(v) if D.is_torch(v) else v, dtype=np.int64) for v in (msort, qsort, zsort)]
+    order = np.ravel_multi_index((ms, qs, zs), shape[:3])
+    order_t = D.as_device(order, dtype=D.torch().int32)
+    st = D.StatusWord()
+    ss, bg = loudest_device(num, hh, int(nreals), int(nloudest), order_t, seed=seed, replay=replay, status=st)
+    _raise_status(st)
+    if like_torch:
+        return ss, bg
+    return D.to_host(ss), D.to_host(bg)
+
+
+def sam_poisson_gwb(dist, hc2, nreals, normal_threshold=1e10, seed=None, replay=None):
+    """hc^2 of the whole population per (F, R), bins in grid order (cyutils.pyx:854-897)."""
+    _check_threshold(normal_threshold)
+    like_torch = D.is_torch(dist)
+    t = D.torch()
+    nf = int(dist.shape[-1])
+    num = D.as_device(dist).reshape(-1, nf)
+    hh = D.as_device(hc2).reshape(-1, nf)
+    nb = int(num.shape[0])
+    gwb = t.empty((nf, int(nreals)), dtype=t.float64, device=num.device)
+    mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
+    rep = None
+    if replay is not None:
+        rep = D.as_device(replay)
+        if tuple(rep.shape) != (nb, nf, int(nreals)):
+            raise ValueError(f"replay must be shaped (B, F, R)=({nb}, {nf}, {nreals}), got {tuple(rep.shape)}")
+    st = D.StatusWord()
+    seed = new_seed() if seed is None else int(seed) & 0xFFFFFFFFFFFFFFFF
+    lib = N.load()
+    ws_bytes = lib.hgb_sam_poisson_gwb_workspace_bytes(nb, nf, int(nreals))
+    ws = D.workspace(ws_bytes, num.device)
+    N.call("hgb_sam_poisson_gwb", N.ptr(num), N.ptr(hh), nb, nf, int(nreals), mode, seed, N.ptr(rep), N.ptr(gwb),
+           N.ptr(ws), int(ws_bytes), st.ptr, N.stream_handle())
+    _raise_status(st)
+    return gwb if like_torch else D.to_host(gwb)
+
+
+def _raise_status(st):
+    code = st.read()
+    if code & N.STATUS_ITERATION_LIMIT:
+        raise RuntimeError("a Poisson sampler exhausted its attempt budget (device status ITERATION_LIMIT)")

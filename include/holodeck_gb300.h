@@ -1,0 +1,255 @@
+/*
+ * holodeck_gb300 C ABI: GB300 (sm_103a) kernels for holodeck's semi-analytic-model
+ * gravitational-wave-background path.
+ *
+ * Conventions shared by every entry point
+ * - All array arguments are DEVICE pointers to C-contiguous float64 (or int32 where
+ *   stated) arrays laid out exactly like the numpy arrays of the holodeck function the
+ *   entry point replaces: (M, Q, Z) grids are m-major, (M, Q, Z, F) grids carry the
+ *   frequency index fastest.
+ * - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).  Every
+ *   call only enqueues work; results are ready once the stream is synchronised.
+ * - `d_status` (may be NULL) is a device int32 word.  Kernels OR HGB_STATUS_* bits into
+ *   it when a bounded device loop runs out or an input check fails on the device; the
+ *   caller zeroes it before the call and reads it after synchronising.
+ * - Functions that need scratch memory take `workspace`/`workspace_bytes`; the matching
+ *   *_workspace_bytes() query returns the size.  No entry point allocates device memory.
+ * - Return value: HGB_OK or an HGB_ERR_* code (argument errors are detected on the
+ *   host before anything is enqueued).  hgb_error_string() describes a code.
+ */
+#ifndef HOLODECK_GB300_H
+#define HOLODECK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes */
+#define HGB_OK 0
+#define HGB_ERR_INVALID_ARGUMENT 1
+#define HGB_ERR_CUDA 2
+#define HGB_ERR_WORKSPACE 3
+
+/* ---- device status bits (OR-ed into *d_status) */
+#define HGB_STATUS_ITERATION_LIMIT 1   /* a bounded sampling / root-finding loop ran out */
+#define HGB_STATUS_INVALID_REDSHIFT 2  /* redz < 0 and != -1 (single_sources.py:95-98) */
+#define HGB_STATUS_TABLE_RANGE 4       /* an interpolation argument left its table */
+#define HGB_STATUS_GRADIENT_NOT_CONVERGED 8  /* scatter gradient solve hit grad_maxiter (scipy only warns) */
+
+/* ---- realization modes for hgb_loudest_hc_from_sorted / hgb_sam_poisson_gwb */
+#define HGB_RNG_PHILOX 0   /* counter-based Philox4x32-10 draws keyed by (seed, bin, realization, frequency) */
+#define HGB_RNG_REPLAY 1   /* consume caller-supplied draws (bit-exact replay of numpy's stream) */
+
+/* Cosmology consumed by the kernels: flat matter + Lambda, no radiation.
+ * Tables are device pointers; they match holodeck's cosmo._grid_z (decreasing),
+ * cosmo._grid_age (increasing, s) and cosmo._grid_dcom (cm)  (sam_cyutils.pyx:476, :494). */
+typedef struct {
+    double H0;              /* [1/s] */
+    double Om0;
+    double Ode0;
+    double age_pref;        /* 2 / (3 H0 sqrt(Ode0))         age(z) = age_pref * asinh(age_c1 (1+z)^-1.5) */
+    double age_c1;          /* sqrt(Ode0 / Om0) */
+    double tz_c2;           /* 1.5 H0 sqrt(Ode0)             z(t) = (age_c1 / sinh(tz_c2 t))^(2/3) - 1 */
+    double age_limit;       /* age(0) rounded through Gyr, the stall threshold of utils.py:46, :1797-1806 */
+    double hubble_distance; /* c / H0 [cm] */
+    const double *grid_z;   /* [grid_size] */
+    const double *grid_age; /* [grid_size] */
+    const double *grid_dcom;/* [grid_size] */
+    int grid_size;
+    /* comoving distance D_C as a function of u = sqrt(1/(1+z)) on u = k / dc_n, k = 0..dc_n:
+     * values [cm] and derivatives dD/du [cm]; cubic Hermite interpolation between nodes */
+    const double *dc_val;   /* [dc_n + 1] */
+    const double *dc_der;   /* [dc_n + 1] */
+    int dc_n;
+} hgb_cosmo;
+
+/* Galaxy / black-hole population model (holodeck/sams/components.py, host_relations.py). */
+#define HGB_GSMF_SCHECHTER 0         /* GSMF_Schechter (components.py:110-172) */
+#define HGB_GSMF_DOUBLE_SCHECHTER 1  /* GSMF_Double_Schechter (components.py:276-330) */
+#define HGB_RATE_GPF_GMT 0           /* GPF_Power_Law / GMT_Power_Law (components.py:520-675) */
+#define HGB_RATE_GMR 1               /* GMR_Illustris (components.py:380-483), optional GMT */
+typedef struct {
+    int gsmf_kind;
+    /* GSMF_Schechter: phi0, phiz, mchar0 [g], mcharz, alpha0, alphaz
+     * GSMF_Double_Schechter: log10_phi1[3], log10_phi2[3], log10_mstar[3], alpha1, alpha2 */
+    double gsmf[11];
+    int rate_kind;
+    int use_gmt;            /* 1 if a GMT is present (always 1 for HGB_RATE_GPF_GMT) */
+    double gpf[6];          /* frac_norm, mref [g], malpha, zbeta, qgamma, max_frac */
+    double gmt[5];          /* time_norm [s], mref [g], malpha, zbeta, qgamma */
+    double gmr[11];         /* norm0 [1/s], normz, malpha0, malphaz, mdelta0, mdeltaz, qgamma0, qgammaz, qgammam, mref_delta [g], mref [g] */
+    double mmb[4];          /* mamp [g], mplaw, mref [g], bulge_frac */
+    int gsmf_uses_mtot, gpf_uses_mtot, gmt_uses_mtot;   /* sam.py:55-59 */
+} hgb_sam_model;
+
+/* ---- library */
+int hgb_version(void);
+const char *hgb_error_string(int code);
+/* last CUDA error text of the calling thread after HGB_ERR_CUDA */
+const char *hgb_last_cuda_error(void);
+
+/* Static binary density before M-Mbulge scatter, plus the galaxy-merger time and the
+ * redshift after the merger (-1 past the age of the Universe).
+ * Replaces Semi_Analytic_Model.static_binary_density, sam.py:280-365 (+ mass_stellar
+ * sam.py:250-278, components.py:132-172, :556-586, :620-675, utils.py:1772-1808).
+ * density/gmt_time/redz_prime are (M, Q, Z); gmt_time/redz_prime are left untouched
+ * when the model has no GMT. */
+int hgb_static_density(const hgb_sam_model *model, const hgb_cosmo *cosmo,
+                       const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                       const double *redz, int n_redz,
+                       double *density, double *gmt_time, double *redz_prime,
+                       int *d_status, void *stream);
+
+/* density[i] = 0 where redz_prime[i] < 0 (sam.py:392-394). */
+int hgb_zero_stalled(double *density, const double *redz_prime, long n, void *stream);
+
+/* ---- M-Mbulge scatter (sam.py:1291-1394, add_scatter_to_masses)
+ * Per redshift slice: Clough-Tocher interpolation of the density from the (log10 m1, log10 m2)
+ * points of the (mtot, mrat) grid onto a (refine*M)^2 regular log grid (gradients by the
+ * minimum-norm-network Gauss-Seidel solve, tolerance 1e-6, 400 sweeps), nearest-point repair of
+ * NaN / negative nodes, Gaussian redistribution W^T G W along both mass axes, bilinear
+ * interpolation back to the points.  The geometry depends only on the grid and is built once on
+ * the host by hgb_scatter_plan_build (HOST pointers), copied to the device by the caller and
+ * passed as hgb_scatter_plan (DEVICE pointers). */
+typedef struct {
+    int n_pts;      /* M*Q points */
+    int n_tri;      /* triangles */
+    int n_nbr;      /* directed point-neighbour entries */
+    int n_grid;     /* refine*M nodes per axis */
+    int n_levels;   /* Gauss-Seidel wavefront levels */
+} hgb_scatter_sizes;
+
+typedef struct {    /* host arrays, sized by hgb_scatter_plan_bounds */
+    double *pts;        /* [n_pts][2] (log10 m1, log10 m2), m-major */
+    int32_t *tri;       /* [n_tri][3] counter-clockwise point indices */
+    double *tri_kappa;  /* [n_tri][3] cross-derivative coefficient of the edge opposite each vertex */
+    double *vtx_qinv;   /* [n_pts][4] inverse normal matrix of the gradient update */
+    int32_t *nbr_ptr;   /* [n_pts+1] */
+    int32_t *nbr_idx;   /* [n_nbr] */
+    double *nbr_w;      /* [n_nbr][4] edge vector and edge vector / length^3 */
+    int32_t *level_ptr; /* [n_levels+1] */
+    int32_t *level_vtx; /* [n_pts] points ordered by level */
+    int32_t *grid_tri;  /* [n_grid^2] containing triangle, -1 outside the hull */
+    double *grid_bary;  /* [n_grid^2][3] barycentric coordinates */
+    int32_t *grid_near; /* [n_grid^2] nearest point */
+    double *grid_axis;  /* [n_grid] log10 mass of the regular grid */
+    double *weights;    /* [n_grid][n_grid] W[source][target] */
+    int32_t *back_idx;  /* [n_pts][2] lower grid cell */
+    double *back_t;     /* [n_pts][2] fractional offsets */
+} hgb_scatter_host_plan;
+
+typedef struct {    /* the same arrays on the device */
+    int n_mtot, n_mrat, n_grid, n_tri, n_levels;
+    const double *pts;
+    const int32_t *tri;
+    const double *tri_kappa;
+    const double *vtx_qinv;
+    const int32_t *nbr_ptr;
+    const int32_t *nbr_idx;
+    const double *nbr_w;
+    const int32_t *level_ptr;
+    const int32_t *level_vtx;
+    const int32_t *grid_tri;
+    const double *grid_bary;
+    const int32_t *grid_near;
+    const double *weights;
+    const int32_t *back_idx;
+    const double *back_t;
+    double grad_tol;    /* 1e-6 in the reference */
+    int grad_maxiter;   /* 400 in the reference */
+} hgb_scatter_plan;
+
+/* Upper bounds of the plan array sizes (n_grid is exact). */
+int hgb_scatter_plan_bounds(int n_mtot, int n_mrat, int refine, hgb_scatter_sizes *out);
+/* Build the geometry on the host; mtot / mrat are HOST arrays; writes the actual sizes. */
+int hgb_scatter_plan_build(const double *mtot, int n_mtot, const double *mrat, int n_mrat, int refine,
+                           double scatter_dex, hgb_scatter_host_plan *plan, hgb_scatter_sizes *sizes);
+size_t hgb_scatter_workspace_bytes(int n_mtot, int n_mrat, int n_redz, int n_grid);
+/* dens (M, Q, Z) is replaced by its scattered version. */
+int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_redz,
+                              void *workspace, size_t workspace_bytes, int *d_status, void *stream);
+
+/* log10 hardening-rate normalisation per (mtot, mrat) cell such that the two-power-law
+ * lifetime equals target_time: Brent root on [-20, 20], xtol 1e-3, rtol 1e-5, 100 iterations
+ * (0 when the interval brackets no root, like scipy's cython brentq).  `norm` (may be NULL)
+ * receives 10**norm_log10, the Fixed_Time_2PL_SAM._norm of hardening.py:1412-1416.
+ * Replaces sam_cyutils.find_2pwl_hardening_norm, sam_cyutils.pyx:289-398. */
+int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const double *mrat, int n,
+                                 double sepa_init, double rchar, double gamma_inner, double gamma_outer,
+                                 int nsteps, double *norm_log10, double *norm, int *d_status, void *stream);
+
+/* x[i] = sqrt(x[i]) (the hc^2 -> hc step of single_sources.py:166-167). */
+int hgb_sqrt_inplace(double *x, long n, void *stream);
+
+/* Differential binary number d^4N/[dlog10M dq dz dlnf] and the redshift at each target
+ * frequency for Fixed_Time_2PL_SAM hardening.  Replaces _dynamic_binary_number_at_fobs_2pwl,
+ * sam_cyutils.pyx:510-781.  redz_final / diff_num are (M, Q, Z, F) and fully written
+ * (-1 / 0 where no target is reached).  fobs_sorted = 1 asserts fobs_orb is ascending. */
+int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                 const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                 const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                 const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                 double *redz_final, double *diff_num, void *stream);
+
+/* Same for Hard_GW (GW-only) hardening.  Replaces _dynamic_binary_number_at_fobs_gw,
+ * sam_cyutils.pyx:788-899.  redz_prime is (M, Q, Z). */
+int hgb_dbn_gw(const double *fobs_orb, int n_freq, const double *nden, const double *mtot, int n_mtot,
+               const double *mrat, int n_mrat, int n_redz, const double *redz_prime,
+               const hgb_cosmo *cosmo, double *redz_final, double *diff_num, void *stream);
+
+/* number (M-1, Q-1, Z-1, F) = 8-vertex mean of dnum x dlog10M dq dz x dlnf.
+ * Replaces _integrate_differential_number_3dx1d, sam_cyutils.pyx:170-216; takes the arguments of
+ * that Cython kernel: log10(mtot) edges, mrat and redz edges, and dln_freq = diff(ln(fobs_orb_edges))
+ * as its Python wrapper (sam_cyutils.pyx:115-167) prepares them. */
+int hgb_integrate_3dx1d(const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat,
+                        const double *redz, int n_redz, const double *dln_freq, int n_freq,
+                        const double *dnum, double *number, void *stream);
+
+/* h2fdf (M-1, Q-1, Z-1, F) = h_s^2 f/df at bin centres from the 3-axis midpoint of redz_final.
+ * Replaces gravwaves.char_strain_sq_from_bin_edges_redz, gravwaves.py:694-724.
+ * gw_src_const is holodeck.utils._GW_SRC_CONST (utils.py:40). */
+int hgb_char_strain_sq(const double *mtot, int n_mtot, const double *mrat, int n_mrat, int n_redz,
+                       const double *fobs_orb_edges, int n_freq, const double *redz_final, double gw_src_const,
+                       const hgb_cosmo *cosmo, double *h2fdf, int *d_status, void *stream);
+
+/* Both of the above in one pass over the (M, Q, Z, F) grids (the sequence of gwb(), sam.py:930-935).
+ * Also flags redz_final values < 0 and != -1 (single_sources.py:95-98) in *d_status. */
+int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat,
+                          const double *redz, int n_redz, const double *fobs_orb_edges, const double *dln_freq,
+                          int n_freq, const double *dnum, const double *redz_final, double gw_src_const,
+                          const hgb_cosmo *cosmo, double *number, double *h2fdf, int *d_status, void *stream);
+
+/* order[k] = flat bin index of the k-th largest h2fdf[..., 0] (single_sources.py:89).
+ * Ties keep ascending bin index. */
+size_t hgb_sort_workspace_bytes(long n_bins);
+int hgb_argsort_f0_desc(const double *h2fdf, long n_bins, int n_freq, int32_t *order,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* Poisson realizations with the loudest-L split.  Replaces cyutils.loudest_hc_from_sorted,
+ * cyutils.pyx:1220-1344: for every realization r and frequency f the bins are visited in
+ * `order`; each bin draws n ~ Poisson(number) (Normal(number, sqrt(number)) above 1e10),
+ * the first `nloud` sources fill hc2ss[f, r, :] and the rest add n*h2fdf to hc2bg[f, r].
+ * number / h2fdf are (B, F) (the (M-1, Q-1, Z-1, F) grids flattened); hc2ss is (F, R, L),
+ * hc2bg (F, R), both fully written.
+ * mode HGB_RNG_PHILOX: draws from Philox4x32-10 keyed by seed.
+ * mode HGB_RNG_REPLAY: replay[(r*F + f)*B + k] is the draw of the k-th sorted bin. */
+size_t hgb_loudest_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode);
+int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n_bins, int n_freq,
+                               int nreals, int nloud, const int32_t *order, int mode, uint64_t seed,
+                               const double *replay, double *hc2ss, double *hc2bg,
+                               void *workspace, size_t workspace_bytes, int *d_status, void *stream);
+
+/* Second-pass GWB without the loudest split.  Replaces cyutils.sam_poisson_gwb,
+ * cyutils.pyx:854-897; gwb is (F, R).  replay[(b*F + f)*R + r] in REPLAY mode (no workspace needed). */
+size_t hgb_sam_poisson_gwb_workspace_bytes(long n_bins, int n_freq, int nreals);
+int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, int n_freq, int nreals,
+                        int mode, uint64_t seed, const double *replay, double *gwb,
+                        void *workspace, size_t workspace_bytes, int *d_status, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HOLODECK_GB300_H */
