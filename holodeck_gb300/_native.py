@@ -64,7 +64,7 @@ class HgbScatterSizes(ctypes.Structure):
 
 
 _SCATTER_ARRAYS = ["pts", "tri", "tri_kappa", "vtx_qinv", "nbr_ptr", "nbr_idx", "nbr_w", "level_ptr", "level_vtx",
-                   "grid_tri", "grid_bary", "grid_near", "grid_axis", "weights", "back_idx", "back_t"]
+                   "grid_tri", "grid_bary", "grid_near", "grid_axis", "weights", "back_idx", "back_t", "back_w"]
 
 
 class HgbScatterHostPlan(ctypes.Structure):
@@ -156,7 +156,7 @@ def check(rc, what):
 #: per 8 key bits); used to report the launch count of a timed region
 KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
-    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 1, "hgb_dbn_gw": 1,
+    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
     "hgb_loudest_hc_from_sorted": 3, "hgb_sam_poisson_gwb": 2,
 }

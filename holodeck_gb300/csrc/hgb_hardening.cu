@@ -1,8 +1,11 @@
 // Binary hardening on the GPU:
 //  * hgb_find_2pwl_hardening_norm: Brent root of the two-power-law lifetime per (mtot, mrat) cell
 //    (holodeck/sams/sam_cyutils.pyx:289-398); one warp per cell.
-//  * hgb_dbn_2pwl: differential binary number for Fixed_Time_2PL_SAM (sam_cyutils.pyx:510-781);
-//    one block per (mtot, mrat) cell, one thread per starting redshift, step tables in shared memory.
+//  * hgb_dbn_2pwl: differential binary number for Fixed_Time_2PL_SAM (sam_cyutils.pyx:510-781) in
+//    two phases: k_dbn_2pwl walks the separation steps (one block per (mtot, mrat) cell, one thread
+//    per starting redshift, step tables in shared memory) and records, per target frequency, the
+//    interpolated time of the bracketing step; k_dbn_2pwl_eval then evaluates redshift, distance,
+//    residence time and number for every bracketed (redz, frequency) element in parallel.
 //  * hgb_dbn_gw: differential binary number for Hard_GW (sam_cyutils.pyx:788-899); one thread per
 //    grid point.
 // FP64 throughout (the hardening integral and the lookback-time -> redshift inversion are the
@@ -263,7 +266,6 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
         if (zi > NI - 2) zi = NI - 2;
         double rage = hgb::interp_between(zk, zg[zi], zg[zi + 1], ag[zi], ag[zi + 1]);
         double gmt = gmt_time[row];
-        double nd = nden[row];
         const double fstop = fmax * (1.0 + zk) * (1.0 + 1e-12);
         int il = 0;
         int fp = 0;                 // first target >= the left frequency (targets ascending)
@@ -319,19 +321,67 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
                 }
                 double new_time = hgb::interp_between(ftarget, fl, fr, time_left, time_right);
                 if (new_time > ag[NI - 1]) break;
-                int ni = hgb::while_while_increasing(il_step, NI, new_time, ag);
-                double new_redz = hgb::interp_between(new_time, ag[ni], ag[ni + 1], zg[ni], zg[ni + 1]);
-                double dcom = hgb::interp_between(new_time, ag[ni], ag[ni + 1], dg[ni], dg[ni + 1]);
-                rf[f] = new_redz;
-                double target_frst_orb = ftarget * (1.0 + new_redz);
-                double sp = cc.ksepa * pow(mt, 1.0 / 3.0) / pow(target_frst_orb, 2.0 / 3.0);
-                double dadt_t = hgb::hard_func_2pwl_gw(cc.c_dadt, mt, mr, sp, norm, a.rchar, a.gi, a.go);
-                double tres = -(2.0 / 3.0) * sp / dadt_t;
-                double dcm = dcom / HGB_CY_MPC;
-                double cosmo_fact = cc.fourpi * (1.0 + new_redz) * (dcm * dcm);
-                dn[f] = nd * tres * cosmo_fact;
+                // phase 1 records the bracket; k_dbn_2pwl_eval turns it into redz_final / diff_num
+                rf[f] = (double)il_step;
+                dn[f] = new_time;
             }
         }
+    }
+}
+
+// Phase 2 of the Fixed_Time_2PL_SAM number: every (redz, frequency) element of a (mtot, mrat) cell
+// whose target was bracketed (sam_cyutils.pyx:731-768).  One block per cell, so the cell's
+// constant powers are taken once and the elements run without divergence.
+__global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restrict__ fobs,
+                                const double *__restrict__ hard_norm, const double *__restrict__ nden,
+                                const double *__restrict__ mtot, const double *__restrict__ mrat,
+                                const double *__restrict__ zgrid_g, const double *__restrict__ agrid_g,
+                                const double *__restrict__ dgrid_g, double *__restrict__ redz_final,
+                                double *__restrict__ diff_num) {
+    extern __shared__ double smem[];
+    const int NI = a.n_interp, NF = a.n_freq;
+    double *zg = smem;
+    double *ag = zg + NI;
+    double *dg = ag + NI;
+    double *ft = dg + NI;
+    const int cell = blockIdx.x;
+    const int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
+    for (int i = threadIdx.x; i < NI; i += blockDim.x) {
+        zg[i] = zgrid_g[i];
+        ag[i] = agrid_g[i];
+        dg[i] = dgrid_g[i];
+    }
+    for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = fobs[i];
+    __shared__ double s_mt3, s_mr12, s_mt13;
+    const double mt = mtot[ii], mr = mrat[jj], norm = hard_norm[cell];
+    if (threadIdx.x == 0) {
+        s_mt3 = pow(mt, 3.0);
+        s_mr12 = pow(1.0 + mr, 2.0);
+        s_mt13 = pow(mt, 1.0 / 3.0);
+    }
+    __syncthreads();
+    const double mt3 = s_mt3, mr12 = s_mr12, mt13 = s_mt13;
+    const long nzf = (long)a.n_redz * NF;
+    const long base = (long)cell * nzf;
+    for (long e = threadIdx.x; e < nzf; e += blockDim.x) {
+        double hint = redz_final[base + e];
+        if (hint < 0.0) continue;   // no bracket: stays -1 / 0
+        const int f = (int)(e % NF);
+        const int kk = (int)(e / NF);
+        const double new_time = diff_num[base + e];
+        int ni = hgb::while_while_increasing((int)hint, NI, new_time, ag);
+        double new_redz = hgb::interp_between(new_time, ag[ni], ag[ni + 1], zg[ni], zg[ni + 1]);
+        double dcom = hgb::interp_between(new_time, ag[ni], ag[ni + 1], dg[ni], dg[ni + 1]);
+        double target_frst_orb = ft[f] * (1.0 + new_redz);
+        double sp = cc.ksepa * mt13 / pow(target_frst_orb, 2.0 / 3.0);
+        double xx = sp / a.rchar;
+        double dadt = -norm * pow(1.0 + xx, -a.go + a.gi) / pow(xx, a.gi - 1.0);
+        dadt += cc.c_dadt * mt3 * mr / (sp * sp * sp) / mr12;
+        double tres = -(2.0 / 3.0) * sp / dadt;
+        double dcm = dcom / HGB_CY_MPC;
+        double cosmo_fact = cc.fourpi * (1.0 + new_redz) * (dcm * dcm);
+        redz_final[base + e] = new_redz;
+        diff_num[base + e] = nden[(long)cell * a.n_redz + kk] * tres * cosmo_fact;
     }
 }
 
@@ -441,6 +491,12 @@ int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sep
                                                                 mrat, redz, gmt_time, cosmo->grid_z,
                                                                 cosmo->grid_age, cosmo->grid_dcom, redz_final,
                                                                 diff_num);
+    int rc = hgb::check_launch();
+    if (rc) return rc;
+    size_t smem2 = sizeof(double) * ((size_t)3 * cosmo->grid_size + n_freq);
+    k_dbn_2pwl_eval<<<blocks, 256, smem2, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden, mtot,
+                                                                  mrat, cosmo->grid_z, cosmo->grid_age,
+                                                                  cosmo->grid_dcom, redz_final, diff_num);
     return hgb::check_launch();
 }
 

@@ -4,29 +4,36 @@
 // cyutils.sam_poisson_gwb (holodeck/cyutils.pyx:854-897).
 //
 // Layout: the (B, F) number and h2fdf grids are gathered once into loudest-first order and
-// transposed to (F, B), so that one frequency's sorted bins are contiguous.  A block owns one
-// frequency, a contiguous chunk of sorted bins and up to RB*RPT realizations (RPT per thread, in
-// registers).  It stages RB bins at a time in shared memory together with their sampler
-// constants -- computed once per bin per block, i.e. amortised over all realizations -- and
-// every thread then walks the tile in sorted order for each of its realizations.  All threads of
-// a warp see the same bin, so the sampler choice is warp-uniform and the zero-expectation bins
-// (most of the grid) cost one shared-memory load per bin per thread, not per draw.
+// transposed to (F, B), so one frequency's sorted bins are contiguous.  A block owns one
+// frequency, up to RB*RPT realizations (RPT per thread, kept in shared memory) and one chunk of
+// bins; a chunk is every nchunk-th tile of RB sorted bins, so chunks carry the same mix of cheap
+// and expensive bins and finish together.  The block stages a tile in shared memory with its
+// per-bin sampler constants -- computed once per bin per block, i.e. amortised over all
+// realizations -- and each thread walks the tile in sorted order for its realizations.  All
+// threads of a warp see the same bin, so the choice of sampler is warp-uniform and bins with zero
+// expectation (most of the grid) cost one shared-memory load per thread.
 //
-// Draws (HGB_RNG_PHILOX): counter-based Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) keyed
-// by the 64-bit seed with counter (sorted bin, realization, frequency, attempt), so results do not
-// depend on the launch shape.  Samplers:
-//   lambda <= 0 or NaN       n = 0 (no draw)
-//   0 < lambda < 10          inversion of one 64-bit uniform against a per-bin table of
-//                            floor(CDF(n) 2^64), n < NT; integer compares only (FP64 beyond NT)
-//   10 <= lambda < 2^22      PTRS, transformed rejection with squeeze (Hormann 1993,
-//                            Insurance: Mathematics and Economics 12, 39-45), FP32 arithmetic,
-//                            acceptance test in the log-pmf form of Loader's saddle-point
-//                            expansion (bd0 + Stirling remainder), so nothing cancels in FP32
-//   2^22 <= lambda <= 1e10   PTRS in FP64
-//   lambda > 1e10            Normal(lambda, sqrt(lambda)) by Box-Muller, as the reference does
-// Background sums accumulate n * h2fdf * 2^100 in FP32 with Kahan compensation (relative error
-// ~1e-7 of hc^2); the loudest slots store the exact float64 h2fdf values.  Every rejection loop
-// stops after a fixed number of attempts and flags HGB_STATUS_ITERATION_LIMIT.
+// Draws (HGB_RNG_PHILOX): counter-based Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) keyed by
+// the 64-bit seed; counters are built from (sorted bin, realization, frequency, stream word), so
+// results do not depend on chunking.  Samplers by expectation lambda:
+//   lambda <= 0 or NaN        n = 0, no draw
+//   lambda < TINY             geometric skipping over a thread's realizations: the gap to the next
+//                             realization with n >= 1 is floor(-ln u / lambda) (P(n = 0) = e^-lambda),
+//                             so one 64-bit uniform usually settles all RPT realizations; a hit
+//                             draws n from the zero-truncated Poisson
+//   TINY <= lambda < 10       inversion of a 64-bit uniform against a per-bin table of
+//                             floor(CDF(n) 2^64) (n = 0) and floor(CDF(n) 2^32) (n >= 1); two
+//                             realizations per Philox call
+//   10 <= lambda < 2^22       PTRS, transformed rejection with squeeze (Hormann 1993, Insurance:
+//                             Mathematics and Economics 12, 39-45) in FP32, acceptance test in the
+//                             log-pmf form of Loader's saddle-point expansion (bd0 + Stirling
+//                             remainder), so nothing cancels in FP32; two realizations' first
+//                             attempts per Philox call
+//   2^22 <= lambda <= 1e10    PTRS in FP64
+//   lambda > 1e10             Normal(lambda, sqrt(lambda)) by Box-Muller, as the reference does
+// Counts are integers; background sums accumulate n * h2fdf * 2^100 in FP32 with Kahan
+// compensation (relative error ~1e-7 of hc^2); the loudest slots hold the exact float64 h2fdf.
+// Every rejection / inversion loop is bounded and flags HGB_STATUS_ITERATION_LIMIT when it runs out.
 //
 // Replay (HGB_RNG_REPLAY): the caller supplies the draws in the reference's order (numpy's PCG64
 // stream); one thread per (frequency, realization) walks all bins sequentially and accumulates in
@@ -39,18 +46,26 @@
 namespace {
 
 constexpr int RB = 128;                  // threads per block == bins per staged tile
-constexpr int RPT = 8;                   // realizations per thread (registers)
+constexpr int RPT = 8;                   // realizations per thread
 constexpr int NT = 24;                   // CDF thresholds per small-lambda bin
+constexpr double TINY = 0.02;            // geometric skipping below this expectation
 constexpr double NORMAL_THRESH = 1e10;   // long(1e10) in cyutils.pyx:1223
 constexpr double PTRS_MIN = 10.0;
 constexpr double PTRS32_MAX = 4194304.0; // 2^22: k stays exact in FP32
 constexpr int MAX_ATTEMPTS = 64;
 constexpr int MAX_INVERSION = 4096;
+// stream words (counter .w) of the different draw families
+constexpr uint32_t W_PAIR = 0u;             // first draw / first PTRS attempt of a realization pair
+constexpr uint32_t W_RETRY = 0x10000000u;   // | attempt: further PTRS attempts of one realization
+constexpr uint32_t W_SKIP = 0x20000000u;    // | step: geometric skipping of a thread's realizations
+constexpr uint32_t W_WIDE = 0x30000000u;    // | attempt: PTRS64 / Normal draws
 constexpr uint32_t DOMAIN_GWB = 0x80000000u;
 constexpr float HSCALE = 0x1.0p100f;     // keeps h2fdf (1e-30 .. 1e-20) far from FP32 subnormals
 constexpr double HSCALE_INV = 0x1.0p-100;
 
-enum BinKind : int { KIND_NONE = 0, KIND_SMALL = 1, KIND_PTRS32 = 2, KIND_PTRS64 = 3, KIND_NORMAL = 4 };
+enum BinKind : int {
+    KIND_NONE = 0, KIND_TINY = 1, KIND_SMALL = 2, KIND_PTRS32 = 3, KIND_PTRS64 = 4, KIND_NORMAL = 5
+};
 
 // ---- Philox4x32-10
 constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u, PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
@@ -71,6 +86,9 @@ __device__ __forceinline__ double u53(uint32_t hi, uint32_t lo) {   // [0, 1)
     return (double)(((uint64_t)hi << 21) ^ (uint64_t)(lo >> 11)) * 0x1.0p-53;
 }
 __device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * 0x1.0p-24f; }   // [0, 1)
+__device__ __forceinline__ unsigned long long w64(uint32_t hi, uint32_t lo) {
+    return ((unsigned long long)hi << 32) | lo;
+}
 
 // log(k!) for k < 16, used by the PTRS acceptance test in the far lower tail
 __constant__ double c_lgam[16] = {
@@ -85,8 +103,9 @@ __constant__ double c_inv[NT] = {
 
 // Per-bin sampler constants of one staged tile, shared by every realization of the block.
 struct Tile {
-    unsigned long long thr0[RB];      // small lambda: floor(CDF(0) 2^64), saturating
-    unsigned int thr[NT][RB];         // small lambda: floor(CDF(n) 2^32), n >= 1 (entry 0 unused)
+    unsigned long long t0[RB];        // floor(e^-lambda 2^64): u < t0 <=> n = 0
+    unsigned long long tskip[RB];     // tiny lambda: floor(e^(-RPT lambda) 2^64): no hit in RPT draws
+    unsigned int thr[NT][RB];         // small lambda: floor(CDF(n) 2^32), n >= 1 (row 0 unused)
     double lam[RB];
     double h[RB];                     // exact h2fdf (for the loudest slots)
     float hs[RB];                     // h2fdf * 2^100 (for the background sums)
@@ -106,20 +125,25 @@ __device__ void bin_setup(Tile &s, int j, double lam, double h) {
     int kind;
     if (!(lam > 0.0)) kind = KIND_NONE;
     else if (lam > NORMAL_THRESH) kind = KIND_NORMAL;
+    else if (lam < TINY) kind = KIND_TINY;
     else if (lam < PTRS_MIN) kind = KIND_SMALL;
     else if (lam < PTRS32_MAX) kind = KIND_PTRS32;
     else kind = KIND_PTRS64;
     s.kind[j] = kind;
-    if (kind == KIND_SMALL) {
+    if (kind == KIND_TINY) {
+        s.t0[j] = sat64(exp(-lam));
+        s.tskip[j] = sat64(exp(-(double)RPT * lam));
+    } else if (kind == KIND_SMALL) {
         double p = exp(-lam);
         double cdf = p;
-        s.thr0[j] = sat64(cdf);
-#pragma unroll 4
-        for (int n = 1; n < NT; n++) {
+        s.t0[j] = sat64(cdf);
+        int n = 1;
+        for (; n < NT && cdf < 1.0; n++) {
             p = p * lam * c_inv[n];
             cdf += p;
             s.thr[n][j] = (unsigned int)(sat64(cdf) >> 32);
         }
+        for (; n < NT; n++) s.thr[n][j] = 0xFFFFFFFFu;
     } else if (kind == KIND_PTRS32) {
         double slam = sqrt(lam);
         double b = 0.931 + 2.53 * slam;
@@ -164,50 +188,53 @@ __device__ __forceinline__ float log_pmf32(int k, float d, float lamf) {
     return -bd0 - 0.5f * logf(6.283185307179586f * kf) - stirl;
 }
 
-// PTRS with FP32 arithmetic; w holds the words of attempt 0 and 1, further attempts draw more.
-__device__ int ptrs32(const Tile &s, int j, uint4 ctr, uint2 key, uint4 w) {
-    const float b = s.b[j], a = s.a[j], vr = s.vr[j], log_inva = s.log_inva[j], frac43 = s.frac43[j];
-    const int lam_int = s.lam_int[j];
-    for (int att = 0; att < MAX_ATTEMPTS; att += 2) {
-        if (att > 0) {
-            ctr.w = (ctr.w & DOMAIN_GWB) | (uint32_t)att;
-            w = philox(ctr, key);
-        }
-#pragma unroll
-        for (int half = 0; half < 2; half++) {
-            float U = u24(half ? w.z : w.x) - 0.5f;
-            float V = u24(half ? w.w : w.y);
-            float us = 0.5f - fabsf(U);
-            if (us < 0.013f && V > us) continue;
-            float kf = floorf((2.0f * a / us + b) * U + frac43);
-            if (!(kf > -1.0e7f && kf < 1.0e7f)) continue;
-            int k = lam_int + (int)kf;
-            if (k < 0) continue;
-            if (us >= 0.07f && V <= vr) return k;
-            float lhs = logf(V) + log_inva - logf(a / (us * us) + b);
-            float rhs;
-            if (k < 16) {
-                double lam = s.lam[j];
-                rhs = (float)(-lam + (double)k * log(lam) - c_lgam[k]);
-            } else {
-                float d = (float)(k - lam_int) - (frac43 - 0.43f);
-                rhs = log_pmf32(k, d, s.lamf[j]);
-            }
-            if (lhs <= rhs) return k;
-        }
+// One PTRS attempt from the uniforms (U word, V word); returns k >= 0 on acceptance, -1 otherwise.
+__device__ __forceinline__ int ptrs32_attempt(const Tile &s, int j, uint32_t wu, uint32_t wv) {
+    const float b = s.b[j], a = s.a[j], frac43 = s.frac43[j];
+    float U = u24(wu) - 0.5f;
+    float V = u24(wv);
+    float us = 0.5f - fabsf(U);
+    if (us < 0.013f && V > us) return -1;
+    float kf = floorf((2.0f * a * __frcp_rn(us) + b) * U + frac43);
+    if (!(kf > -1.0e7f && kf < 1.0e7f)) return -1;
+    int k = s.lam_int[j] + (int)kf;
+    if (k < 0) return -1;
+    if (us >= 0.07f && V <= s.vr[j]) return k;
+    float lhs = logf(V) + s.log_inva[j] - logf(a / (us * us) + b);
+    float rhs;
+    if (k < 16) {
+        double lam = s.lam[j];
+        rhs = (float)(-lam + (double)k * log(lam) - c_lgam[k]);
+    } else {
+        float d = (float)(k - s.lam_int[j]) - (frac43 - 0.43f);
+        rhs = log_pmf32(k, d, s.lamf[j]);
     }
-    return -1;
+    return (lhs <= rhs) ? k : -1;
+}
+
+// Further PTRS attempts of realization r after a rejected first attempt.
+__device__ int ptrs32_retry(const Tile &s, int j, uint32_t kb, uint32_t r, uint32_t f, uint32_t dom, uint2 key,
+                            int *d_status) {
+    for (int att = 1; att < MAX_ATTEMPTS; att++) {
+        uint4 w = philox(make_uint4(kb, r, f, dom | W_RETRY | (uint32_t)att), key);
+        int k = ptrs32_attempt(s, j, w.x, w.y);
+        if (k >= 0) return k;
+        k = ptrs32_attempt(s, j, w.z, w.w);
+        if (k >= 0) return k;
+    }
+    hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+    return (int)floor(s.lam[j] + 0.5);
 }
 
 // PTRS in FP64 for 2^22 <= lambda <= 1e10
-__device__ double ptrs64(uint4 ctr, uint2 key, double lam) {
+__device__ double ptrs64(uint4 ctr, uint2 key, double lam, int *d_status) {
     double slam = sqrt(lam), loglam = log(lam);
     double b = 0.931 + 2.53 * slam;
     double a = -0.059 + 0.02483 * b;
     double inva = 1.1239 + 1.1328 / (b - 3.4);
     double vr = 0.9277 - 3.6224 / (b - 2.0);
     for (int att = 0; att < MAX_ATTEMPTS; att++) {
-        ctr.w = (ctr.w & DOMAIN_GWB) | (uint32_t)att;
+        ctr.w = (ctr.w & 0xF0000000u) | (uint32_t)att;
         uint4 w = philox(ctr, key);
         double U = u53(w.x, w.y) - 0.5;
         double V = u53(w.z, w.w);
@@ -217,55 +244,52 @@ __device__ double ptrs64(uint4 ctr, uint2 key, double lam) {
         if (k < 0.0 || (us < 0.013 && V > us)) continue;
         if (log(V) + log(inva) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
     }
-    return -1.0;
+    hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+    return floor(lam + 0.5);
 }
 
-// Small lambda beyond the threshold table: continue the CDF in FP64.
-__device__ int small_tail(double lam, unsigned long long u, int *d_status) {
+// Count of a small-lambda bin from a 64-bit uniform (u >= t0 already known to mean n >= 1).
+__device__ __forceinline__ int small_count(const Tile &s, int j, unsigned long long u, int *d_status) {
+    int n = 1;
+    const uint32_t hi = (uint32_t)(u >> 32);
+    while (n < NT && hi >= s.thr[n][j]) n++;
+    if (n < NT) return n;
+    // beyond the table: continue the CDF in FP64
+    double lam = s.lam[j];
     double uu = (double)(u >> 11) * 0x1.0p-53;
     double p = exp(-lam);
     double cdf = p;
-    int n = 0;
-    while (uu >= cdf && n < MAX_INVERSION) {
+    int m = 0;
+    while (uu >= cdf && m < MAX_INVERSION) {
+        m++;
+        p *= lam / m;
+        cdf += p;
+    }
+    if (m >= MAX_INVERSION) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+    return m < NT ? NT : m;
+}
+
+// Zero-truncated Poisson count for a tiny-lambda hit, by inversion in FP64 from a 53-bit uniform.
+__device__ int truncated_count(double lam, double v, int *d_status) {
+    double e = exp(-lam);
+    double p = lam * e / (1.0 - e);   // P(n = 1 | n >= 1)
+    double cdf = p;
+    int n = 1;
+    while (v >= cdf && n < MAX_INVERSION) {
         n++;
         p *= lam / n;
         cdf += p;
     }
-    if (n < NT) n = NT;
     if (n >= MAX_INVERSION) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
     return n;
 }
 
-// One draw of sorted bin j for the given counter.  Returns the count (exact integer except in the
-// Normal branch, where it is the reference's real-valued draw).
-__device__ __forceinline__ double draw(const Tile &s, int j, int kind, uint4 ctr, uint2 key, int *d_status) {
-    uint4 w = philox(ctr, key);
-    if (kind == KIND_SMALL) {
-        unsigned long long u = ((unsigned long long)w.x << 32) | w.y;
-        if (u < s.thr0[j]) return 0.0;
-        int n = 1;
-        while (n < NT && w.x >= s.thr[n][j]) n++;
-        if (n == NT) n = small_tail(s.lam[j], u, d_status);
-        return (double)n;
-    }
-    if (kind == KIND_PTRS32) {
-        int k = ptrs32(s, j, ctr, key, w);
-        if (k < 0) {
-            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-            return floor(s.lam[j] + 0.5);
-        }
-        return (double)k;
-    }
+// Real-valued draw for the PTRS64 / Normal kinds.
+__device__ double draw_wide(const Tile &s, int j, int kind, uint4 ctr, uint2 key, int *d_status) {
     double lam = s.lam[j];
-    if (kind == KIND_PTRS64) {
-        double k = ptrs64(ctr, key, lam);
-        if (k < 0.0) {
-            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-            return floor(lam + 0.5);
-        }
-        return k;
-    }
+    if (kind == KIND_PTRS64) return ptrs64(ctr, key, lam, d_status);
     // Normal branch (cyutils.pyx:1328-1330)
+    uint4 w = philox(ctr, key);
     double u1 = 1.0 - u53(w.x, w.y);   // (0, 1]
     double u2 = u53(w.z, w.w);
     double z = sqrt(-2.0 * log(u1)) * cos(2.0 * HGB_PI * u2);
@@ -293,32 +317,66 @@ __global__ void k_gather_sorted(const double *__restrict__ number, const double 
 }
 
 struct LoudArgs {
-    long nb;        // bins
-    int nf, nr, nl; // frequencies, realizations, loudest
-    long chunk;     // sorted bins per block (multiple of RB)
-    int nchunk;
+    long nb;          // bins
+    int nf, nr, nl;   // frequencies, realizations, loudest slots
+    int nchunk;       // chunk c holds tiles c, c + nchunk, c + 2 nchunk, ...
     uint2 key;
 };
 
-// Per-realization state of a block lives in shared memory, indexed [slot][thread]: the loops over
-// a thread's realizations stay rolled (small code, no instruction-cache misses) and the state is
-// touched only when a bin yields at least one source.
+// Per-realization state of a block, indexed [slot][thread].
 struct RealState {
     float acc[RPT][RB];
     float comp[RPT][RB];
     int nfill[RPT][RB];
 };
 
-__device__ __forceinline__ void take_count(RealState &st, int i, double num, double h, float hs, int nl,
-                                           double *ss) {
-    int t = threadIdx.x;
-    int nfill = st.nfill[i][t];
-    while (nfill < nl && num > 0.0) {
-        ss[nfill] = h;
-        num -= 1.0;
-        nfill++;
+// Output rows of one chunk: loudest values (and their sorted positions when chunks are merged),
+// the number of filled slots and the background sum.
+struct LoudOut {
+    double *ss;     // [(c * nf + f) * nr + r][nl]
+    int *pos;       // same shape, or NULL when there is one chunk
+    double *bg;     // [(c * nf + f) * nr + r]
+    int *cnt;       // same, or NULL
+};
+
+template <bool LOUD>
+__device__ __forceinline__ void take(RealState &st, int i, int n, double h, float hs, int nl, int kpos, double *ss,
+                                     int *pos) {
+    const int t = threadIdx.x;
+    if (LOUD) {
+        int nfill = st.nfill[i][t];
+        while (nfill < nl && n > 0) {
+            ss[nfill] = h;
+            if (pos) pos[nfill] = kpos;
+            n--;
+            nfill++;
+        }
+        st.nfill[i][t] = nfill;
     }
-    st.nfill[i][t] = nfill;
+    if (n > 0) {
+        float acc = st.acc[i][t], comp = st.comp[i][t];
+        kahan_add(acc, comp, (float)n * hs);
+        st.acc[i][t] = acc;
+        st.comp[i][t] = comp;
+    }
+}
+
+// Real-valued counts (PTRS64 / Normal) follow cyutils.pyx:1333-1342 literally.
+template <bool LOUD>
+__device__ __forceinline__ void take_real(RealState &st, int i, double num, double h, float hs, int nl, int kpos,
+                                          double *ss, int *pos) {
+    const int t = threadIdx.x;
+    if (LOUD) {
+        if (num < 1.0) return;
+        int nfill = st.nfill[i][t];
+        while (nfill < nl && num > 0.0) {
+            ss[nfill] = h;
+            if (pos) pos[nfill] = kpos;
+            num -= 1.0;
+            nfill++;
+        }
+        st.nfill[i][t] = nfill;
+    }
     if (num != 0.0) {
         float acc = st.acc[i][t], comp = st.comp[i][t];
         kahan_add(acc, comp, (float)(num * (double)hs));
@@ -327,107 +385,164 @@ __device__ __forceinline__ void take_count(RealState &st, int i, double num, dou
     }
 }
 
-// grid (chunk, frequency, realization group); RB threads, up to RPT realizations each.
-// nchunk == 1 writes hc2ss / hc2bg directly; otherwise per-chunk partials (slots, count, sum).
-__global__ void __launch_bounds__(RB) k_loudest_philox(LoudArgs a, const double *__restrict__ lam_s,
-                                                       const double *__restrict__ h_s, double *__restrict__ out_ss,
-                                                       double *__restrict__ out_bg, int *__restrict__ out_cnt,
-                                                       int *d_status) {
+// The realization kernel.  LOUD: loudest split over sorted bins (lam / h are the gathered (F, B)
+// arrays); otherwise the second-pass GWB over bins in grid order (lam / h are the (B, F) grids).
+// grid (chunk, frequency, realization group), RB threads.
+template <bool LOUD>
+__global__ void __launch_bounds__(RB, 6) k_realize(LoudArgs a, const double *__restrict__ lam_in,
+                                                const double *__restrict__ h_in, LoudOut out, int *d_status) {
     __shared__ Tile s;
     __shared__ RealState st;
     const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
     const int r0 = blockIdx.z * RB * RPT + t;
-    int rpt = 0;   // realizations owned by this thread: r0 + i*RB, i < rpt
+    const uint32_t dom = LOUD ? 0u : DOMAIN_GWB;
+    int rpt = 0;   // realizations of this thread: r0 + i * RB, i < rpt
     while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
-    const long b0 = (long)c * a.chunk;
-    long b1 = b0 + a.chunk;
-    if (b1 > a.nb) b1 = a.nb;
-    const double *lam_f = lam_s + (long)f * a.nb;
-    const double *h_f = h_s + (long)f * a.nb;
-    const long row0 = ((long)c * a.nf + f) * a.nr + r0;   // output row of slot 0; slot i adds i*RB
+    const long row0 = ((long)c * a.nf + f) * a.nr + r0;   // output row of slot 0; slot i adds i * RB
     for (int i = 0; i < RPT; i++) {
         st.acc[i][t] = 0.0f;
         st.comp[i][t] = 0.0f;
         st.nfill[i][t] = 0;
     }
-    for (long base = b0; base < b1; base += RB) {
-        const int nt = (int)((b1 - base) < RB ? (b1 - base) : RB);
+    const long ntiles = (a.nb + RB - 1) / RB;
+    for (long tile = c; tile < ntiles; tile += a.nchunk) {
+        const long base = tile * RB;
+        const int nt = (int)((a.nb - base) < RB ? (a.nb - base) : RB);
         __syncthreads();
-        if (t < nt) bin_setup(s, t, lam_f[base + t], h_f[base + t]);
+        if (t < nt) {
+            const long b = base + t;
+            if (LOUD) bin_setup(s, t, lam_in[(long)f * a.nb + b], h_in[(long)f * a.nb + b]);
+            else bin_setup(s, t, lam_in[b * a.nf + f], h_in[b * a.nf + f]);
+        }
         __syncthreads();
+        if (rpt == 0) continue;
         for (int j = 0; j < nt; j++) {
             const int kind = s.kind[j];
             if (kind == KIND_NONE) continue;
             const uint32_t kb = (uint32_t)(base + j);
-            if (kind == KIND_SMALL) {
-                const unsigned long long t0 = s.thr0[j];
+            const int kpos = (int)(base + j);
+            const double h = s.h[j];
+            const float hs = s.hs[j];
+            if (kind == KIND_TINY) {
+                // geometric skipping over the thread's realizations
+                uint4 w = philox(make_uint4(kb, (uint32_t)r0, (uint32_t)f, dom | W_SKIP), a.key);
+                unsigned long long u = w64(w.x, w.y);
+                if (rpt == RPT && u < s.tskip[j]) continue;
+                const double lam = s.lam[j];
+                int i = 0;
+                for (int step = 0; step < 2 * RPT + 2; step++) {
+                    if (step > 0) {
+                        w = philox(make_uint4(kb, (uint32_t)r0, (uint32_t)f, dom | W_SKIP | (uint32_t)step), a.key);
+                        u = w64(w.x, w.y);
+                    }
+                    double uu = ((double)(u >> 11) + 1.0) * 0x1.0p-53;   // (0, 1]
+                    double gap = floor(-log(uu) / lam);
+                    if (gap >= (double)(rpt - i)) break;
+                    i += (int)gap;
+                    int n = truncated_count(lam, u53(w.z, w.w), d_status);
+                    take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
+                               out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
+                    i++;
+                    if (i >= rpt) break;
+                }
+            } else if (kind == KIND_SMALL) {
+                const unsigned long long t0 = s.t0[j];
 #pragma unroll 1
-                for (int i = 0; i < rpt; i++) {
-                    const int r = r0 + i * RB;
-                    uint4 w = philox(make_uint4(kb, (uint32_t)r, (uint32_t)f, 0u), a.key);
-                    unsigned long long u = ((unsigned long long)w.x << 32) | w.y;
-                    if (u < t0) continue;
-                    int n = 1;
-                    while (n < NT && w.x >= s.thr[n][j]) n++;
-                    if (n == NT) n = small_tail(s.lam[j], u, d_status);
-                    take_count(st, i, (double)n, s.h[j], s.hs[j], a.nl, out_ss + (row0 + (long)i * RB) * a.nl);
+                for (int i = 0; i < rpt; i += 2) {
+                    uint4 w = philox(make_uint4(kb, (uint32_t)(r0 + i * RB), (uint32_t)f, dom | W_PAIR), a.key);
+                    unsigned long long u = w64(w.x, w.y);
+                    if (u >= t0) {
+                        int n = small_count(s, j, u, d_status);
+                        take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
+                                   out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
+                    }
+                    u = w64(w.z, w.w);
+                    if (i + 1 < rpt && u >= t0) {
+                        int n = small_count(s, j, u, d_status);
+                        take<LOUD>(st, i + 1, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)(i + 1) * RB) * a.nl,
+                                   out.pos ? out.pos + (row0 + (long)(i + 1) * RB) * a.nl : nullptr);
+                    }
                 }
             } else if (kind == KIND_PTRS32) {
 #pragma unroll 1
-                for (int i = 0; i < rpt; i++) {
-                    const int r = r0 + i * RB;
-                    uint4 ctr = make_uint4(kb, (uint32_t)r, (uint32_t)f, 0u);
-                    int n = ptrs32(s, j, ctr, a.key, philox(ctr, a.key));
-                    if (n < 0) {
-                        hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-                        n = (int)floor(s.lam[j] + 0.5);
+                for (int i = 0; i < rpt; i += 2) {
+                    const uint32_t ra = (uint32_t)(r0 + i * RB);
+                    uint4 w = philox(make_uint4(kb, ra, (uint32_t)f, dom | W_PAIR), a.key);
+                    int n = ptrs32_attempt(s, j, w.x, w.y);
+                    if (n < 0) n = ptrs32_retry(s, j, kb, ra, (uint32_t)f, dom, a.key, d_status);
+                    take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
+                               out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
+                    if (i + 1 < rpt) {
+                        n = ptrs32_attempt(s, j, w.z, w.w);
+                        if (n < 0) n = ptrs32_retry(s, j, kb, ra + RB, (uint32_t)f, dom, a.key, d_status);
+                        take<LOUD>(st, i + 1, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)(i + 1) * RB) * a.nl,
+                                   out.pos ? out.pos + (row0 + (long)(i + 1) * RB) * a.nl : nullptr);
                     }
-                    take_count(st, i, (double)n, s.h[j], s.hs[j], a.nl, out_ss + (row0 + (long)i * RB) * a.nl);
                 }
             } else {
 #pragma unroll 1
                 for (int i = 0; i < rpt; i++) {
-                    const int r = r0 + i * RB;
-                    double num = draw(s, j, kind, make_uint4(kb, (uint32_t)r, (uint32_t)f, 0u), a.key, d_status);
-                    if (num < 1.0) continue;   // cyutils.pyx:1333-1334
-                    take_count(st, i, num, s.h[j], s.hs[j], a.nl, out_ss + (row0 + (long)i * RB) * a.nl);
+                    const uint32_t r = (uint32_t)(r0 + i * RB);
+                    double num = draw_wide(s, j, kind, make_uint4(kb, r, (uint32_t)f, dom | W_WIDE), a.key, d_status);
+                    take_real<LOUD>(st, i, num, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
+                                    out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
                 }
             }
         }
     }
     for (int i = 0; i < rpt; i++) {
         const long row = row0 + (long)i * RB;
-        double *ss = out_ss + row * a.nl;
-        const int nfill = st.nfill[i][t];
-        for (int l = nfill; l < a.nl; l++) ss[l] = 0.0;
-        out_bg[row] = ((double)st.acc[i][t] - (double)st.comp[i][t]) * HSCALE_INV;
-        if (out_cnt) out_cnt[row] = nfill;
+        if (LOUD) {
+            const int nfill = st.nfill[i][t];
+            double *ss = out.ss + row * a.nl;
+            for (int l = nfill; l < a.nl; l++) ss[l] = 0.0;
+            if (out.cnt) out.cnt[row] = nfill;
+        }
+        out.bg[row] = ((double)st.acc[i][t] - (double)st.comp[i][t]) * HSCALE_INV;
     }
 }
 
-// Merge per-chunk partials in chunk order: earlier chunks hold louder bins.
-__global__ void k_loudest_merge(LoudArgs a, const double *__restrict__ part_ss, const double *__restrict__ part_bg,
-                                const int *__restrict__ part_cnt, double *__restrict__ hc2ss,
-                                double *__restrict__ hc2bg) {
+// Merge per-chunk partials: the global loudest slots are the smallest sorted positions among the
+// chunks' own loudest lists (each list is in position order); every other listed source and every
+// chunk background goes to the background.
+__global__ void k_loudest_merge(LoudArgs a, LoudOut part, double *__restrict__ hc2ss, double *__restrict__ hc2bg) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long)a.nf * a.nr) return;
+    const long stride = (long)a.nf * a.nr;
     double *out = hc2ss + idx * a.nl;
-    int filled = 0;
+    // heads[c]: next unread entry of chunk c's list (chunks <= 255, lists <= nl <= 255)
+    unsigned char heads[256];
+    for (int c = 0; c < a.nchunk; c++) heads[c] = 0;
+    for (int l = 0; l < a.nl; l++) {
+        int best = -1, bpos = 0x7FFFFFFF;
+        for (int c = 0; c < a.nchunk; c++) {
+            long row = (long)c * stride + idx;
+            if (heads[c] < part.cnt[row]) {
+                int p = part.pos[row * a.nl + heads[c]];
+                if (p < bpos) {
+                    bpos = p;
+                    best = c;
+                }
+            }
+        }
+        if (best < 0) {
+            out[l] = 0.0;
+            continue;
+        }
+        long row = (long)best * stride + idx;
+        out[l] = part.ss[row * a.nl + heads[best]];
+        heads[best]++;
+    }
     double bg = 0.0;
     for (int c = 0; c < a.nchunk; c++) {
-        long fr = (long)c * a.nf * a.nr + idx;
-        int cnt = part_cnt[fr];
-        const double *ps = part_ss + fr * a.nl;
-        for (int j = 0; j < cnt; j++) {
-            if (filled < a.nl) out[filled++] = ps[j];
-            else bg += ps[j];
-        }
-        bg += part_bg[fr];
+        long row = (long)c * stride + idx;
+        for (int e = heads[c]; e < part.cnt[row]; e++) bg += part.ss[row * a.nl + e];
+        bg += part.bg[row];
     }
-    for (int l = filled; l < a.nl; l++) out[l] = 0.0;
     hc2bg[idx] = bg;
 }
 
+// Replay: thread per (frequency, realization), sequential over the sorted bins (cyutils.pyx:1312-1344).
 __global__ void k_loudest_replay(long nb, int nf, int nr, int nl, const double *__restrict__ h_s,
                                  const double *__restrict__ replay, double *__restrict__ hc2ss,
                                  double *__restrict__ hc2bg) {
@@ -452,56 +567,6 @@ __global__ void k_loudest_replay(long nb, int nf, int nr, int nl, const double *
         sum = __dadd_rn(sum, __dmul_rn(num, cur));
     }
     hc2bg[idx] = sum;
-}
-
-// ---- second-pass GWB (cyutils.pyx:854-897): bins in grid order, no loudest split.
-// grid (chunk, frequency, realization group); partial sums per chunk, reduced in chunk order.
-__global__ void __launch_bounds__(RB) k_gwb_philox(LoudArgs a, const double *__restrict__ number,
-                                                   const double *__restrict__ hc2, double *__restrict__ part,
-                                                   int *d_status) {
-    __shared__ Tile s;
-    __shared__ RealState st;
-    const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
-    const int r0 = blockIdx.z * RB * RPT + t;
-    int rpt = 0;
-    while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
-    const long b0 = (long)c * a.chunk;
-    long b1 = b0 + a.chunk;
-    if (b1 > a.nb) b1 = a.nb;
-    for (int i = 0; i < RPT; i++) {
-        st.acc[i][t] = 0.0f;
-        st.comp[i][t] = 0.0f;
-    }
-    for (long base = b0; base < b1; base += RB) {
-        const int nt = (int)((b1 - base) < RB ? (b1 - base) : RB);
-        __syncthreads();
-        if (t < nt) {
-            long b = base + t;
-            bin_setup(s, t, number[b * a.nf + f], hc2[b * a.nf + f]);
-        }
-        __syncthreads();
-        for (int j = 0; j < nt; j++) {
-            const int kind = s.kind[j];
-            if (kind == KIND_NONE) continue;
-            const float hs = s.hs[j];
-            const uint32_t kb = (uint32_t)(base + j);
-#pragma unroll 1
-            for (int i = 0; i < rpt; i++) {
-                const int r = r0 + i * RB;
-                double num = draw(s, j, kind, make_uint4(kb, (uint32_t)r, (uint32_t)f, DOMAIN_GWB), a.key, d_status);
-                if (num != 0.0) {
-                    float acc = st.acc[i][t], comp = st.comp[i][t];
-                    kahan_add(acc, comp, (float)(num * (double)hs));
-                    st.acc[i][t] = acc;
-                    st.comp[i][t] = comp;
-                }
-            }
-        }
-    }
-    for (int i = 0; i < rpt; i++) {
-        const int r = r0 + i * RB;
-        part[((long)c * a.nf + f) * a.nr + r] = ((double)st.acc[i][t] - (double)st.comp[i][t]) * HSCALE_INV;
-    }
 }
 
 __global__ void k_gwb_reduce(int nchunk, long nfr, const double *__restrict__ part, double *__restrict__ gwb) {
@@ -531,17 +596,17 @@ int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
 int choose_nchunk(long nb, int nf, int nr) {
     long blocks = (long)n_rgroups(nr) * nf;
-    long target = 152L * 10;   // about two waves of resident blocks on 152 SMs
+    long target = 152L * 7 * 2;   // two waves of resident blocks on 152 SMs
     long nchunk = hgb::ceil_div(target, blocks);
-    long maxc = hgb::ceil_div(nb, 16L * RB);
+    long maxc = hgb::ceil_div(nb, 8L * RB);
     if (nchunk > maxc) nchunk = maxc;
     if (nchunk < 1) nchunk = 1;
-    if (nchunk > 256) nchunk = 256;
+    if (nchunk > 255) nchunk = 255;
     return (int)nchunk;
 }
 
 struct LoudLayout {
-    size_t off_lam, off_h, off_ss, off_bg, off_cnt, total;
+    size_t off_lam, off_h, off_ss, off_pos, off_bg, off_cnt, total;
     int nchunk;
 };
 
@@ -555,8 +620,11 @@ LoudLayout loud_layout(long nb, int nf, int nr, int nl, int mode) {
     o += align256(sizeof(double) * nb * nf);
     if (L.nchunk > 1) {
         long n = (long)L.nchunk * nf * nr;
+        long m = n * (nl > 0 ? nl : 1);
         L.off_ss = o;
-        o += align256(sizeof(double) * n * (nl > 0 ? nl : 1));
+        o += align256(sizeof(double) * m);
+        L.off_pos = o;
+        o += align256(sizeof(int) * m);
         L.off_bg = o;
         o += align256(sizeof(double) * n);
         L.off_cnt = o;
@@ -573,8 +641,6 @@ LoudArgs make_args(long nb, int nf, int nr, int nl, int nchunk, uint64_t seed) {
     a.nr = nr;
     a.nl = nl;
     a.nchunk = nchunk;
-    a.chunk = hgb::ceil_div(hgb::ceil_div(nb, nchunk), RB) * RB;
-    a.nchunk = (int)hgb::ceil_div(nb, a.chunk);
     a.key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
     return a;
 }
@@ -594,6 +660,7 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
                                int *d_status, void *stream) {
     HGB_CHECK_ARG(number && h2fdf && order && hc2bg && n_bins >= 0 && n_freq >= 1 && nreals >= 0 && nloud >= 0);
     HGB_CHECK_ARG(nloud == 0 || hc2ss);
+    HGB_CHECK_ARG(nloud <= 255);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || replay);
     HGB_CHECK_ARG(n_bins < (1L << 31) && n_freq <= 65535 && nreals < (1 << 30));
@@ -621,19 +688,17 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
     }
     LoudArgs a = make_args(n_bins, n_freq, nreals, nloud, L.nchunk, seed);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
-    double *ss_dummy = hc2ss;
     if (a.nchunk == 1) {
-        k_loudest_philox<<<grid, RB, 0, st>>>(a, lam_s, h_s, ss_dummy, hc2bg, nullptr, d_status);
+        LoudOut o{hc2ss, nullptr, hc2bg, nullptr};
+        k_realize<true><<<grid, RB, 0, st>>>(a, lam_s, h_s, o, d_status);
         return hgb::check_launch();
     }
-    double *pss = (double *)(w + L.off_ss);
-    double *pbg = (double *)(w + L.off_bg);
-    int *pcnt = (int *)(w + L.off_cnt);
-    k_loudest_philox<<<grid, RB, 0, st>>>(a, lam_s, h_s, pss, pbg, pcnt, d_status);
+    LoudOut part{(double *)(w + L.off_ss), (int *)(w + L.off_pos), (double *)(w + L.off_bg), (int *)(w + L.off_cnt)};
+    k_realize<true><<<grid, RB, 0, st>>>(a, lam_s, h_s, part, d_status);
     rc = hgb::check_launch();
     if (rc) return rc;
     long nt = (long)n_freq * nreals;
-    k_loudest_merge<<<(unsigned)hgb::ceil_div(nt, 256), 256, 0, st>>>(a, pss, pbg, pcnt, hc2ss, hc2bg);
+    k_loudest_merge<<<(unsigned)hgb::ceil_div(nt, 128), 128, 0, st>>>(a, part, hc2ss, hc2bg);
     return hgb::check_launch();
 }
 
@@ -665,12 +730,12 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
         return HGB_ERR_WORKSPACE;
     LoudArgs a = make_args(n_bins, n_freq, nreals, 0, choose_nchunk(n_bins, n_freq, nreals), seed);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
-    double *part = (double *)workspace;
-    k_gwb_philox<<<grid, RB, 0, st>>>(a, number, hc2, part, d_status);
+    LoudOut o{nullptr, nullptr, (double *)workspace, nullptr};
+    k_realize<false><<<grid, RB, 0, st>>>(a, number, hc2, o, d_status);
     int rc = hgb::check_launch();
     if (rc) return rc;
     long nfr = (long)n_freq * nreals;
-    k_gwb_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, part, gwb);
+    k_gwb_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, (double *)workspace, gwb);
     return hgb::check_launch();
 }
 

@@ -9,8 +9,9 @@
 //   2. k_clough_tocher: the C1 piecewise-cubic Clough-Tocher interpolant (centroid split) at every
 //      node of the regular (log m1, log m2) grid; NaN outside the hull; NaN or negative values are
 //      replaced by the value of the nearest point.
-//   3. k_gemm_f64 twice: out = W^T G W, the Gaussian redistribution along both mass axes.
-//   4. k_back: bilinear interpolation of the redistributed grid back to the points.
+//   3. k_back_dot: the Gaussian redistribution W^T (W^T G) as the reference computes it (see
+//      hgb_add_scatter_to_masses) followed by the bilinear interpolation back to the points, fused
+//      into one dot product per (point, slice) with the plan's per-point row of (W W).
 // FP64 throughout; built with -fmad=false.
 #include <math.h>
 
@@ -142,77 +143,29 @@ __global__ void k_clough_tocher(hgb_scatter_plan P, const double *__restrict__ v
         val = clough_tocher(P, r, lam, f, g);
     }
     if (isnan(val) || val < 0.0) val = f[P.grid_near[node]];   // sam.py:1367-1376
-    grid[z * NN + node] = val;
+    // stored transposed, [z][b][a], so that a point's two m2-columns are contiguous rows
+    const long a = node / P.n_grid, b = node % P.n_grid;
+    grid[z * NN + b * P.n_grid + a] = val;
 }
 
-// ---- 3. batched FP64 GEMM  C[b] = op(X) Y   (N x N), tiles 64 x 64 x 16, 4 x 4 outputs per thread
-// X_T: X element (row, k) = X[k * N + row] (transposed access); X / Y batch strides may be 0 (shared).
-template <bool X_T>
-__global__ void __launch_bounds__(256) k_gemm_f64(int N, const double *__restrict__ X, long sx,
-                                                  const double *__restrict__ Y, long sy, double *__restrict__ C, long sc) {
-    __shared__ double Xs[16][64 + 1];
-    __shared__ double Ys[16][64 + 1];
-    const int b = blockIdx.z;
-    const double *Xb = X + (long)b * sx;
-    const double *Yb = Y + (long)b * sy;
-    double *Cb = C + (long)b * sc;
-    const int row0 = blockIdx.y * 64, col0 = blockIdx.x * 64;
-    const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
-    double acc[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
-    for (int k0 = 0; k0 < N; k0 += 16) {
-        for (int e = threadIdx.x; e < 16 * 64; e += 256) {
-            int kk = e / 64, rr = e % 64;
-            int row = row0 + rr, k = k0 + kk;
-            double xv = 0.0;
-            if (row < N && k < N) xv = X_T ? Xb[(long)k * N + row] : Xb[(long)row * N + k];
-            Xs[kk][rr] = xv;
-            int col = col0 + rr;
-            Ys[kk][rr] = (col < N && k < N) ? Yb[(long)k * N + col] : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < 16; kk++) {
-            double xr[4], yc[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) xr[i] = Xs[kk][tr * 4 + i];
-#pragma unroll
-            for (int j = 0; j < 4; j++) yc[j] = Ys[kk][tc * 4 + j];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] += xr[i] * yc[j];
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        int row = row0 + tr * 4 + i;
-        if (row >= N) continue;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            int col = col0 + tc * 4 + j;
-            if (col < N) Cb[(long)row * N + col] = acc[i][j];
-        }
-    }
-}
-
-// ---- 4. bilinear interpolation back to the points
-__global__ void k_back(hgb_scatter_plan P, const double *__restrict__ grid, int nz, double *__restrict__ dens) {
+// ---- 3+4. redistribution and bilinear interpolation back to the points, as one dot product per
+// (point, slice): out = sum_j bw_i[j] ((1 - ty) G[j][b] + ty G[j][b + 1]); one warp per output.
+__global__ void k_back_dot(hgb_scatter_plan P, const double *__restrict__ gridT, int nz, double *__restrict__ dens) {
     const int n = P.n_mtot * P.n_mrat;
-    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)n * nz) return;
-    const int i = (int)(idx / nz), z = (int)(idx % nz);
-    const long NN = (long)P.n_grid * P.n_grid;
-    const double *G = grid + z * NN;
-    const int a = P.back_idx[2 * i], b = P.back_idx[2 * i + 1];
-    const double tx = P.back_t[2 * i], ty = P.back_t[2 * i + 1];
+    const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= (long)n * nz) return;
+    const int i = (int)(warp / nz), z = (int)(warp % nz);
     const long N = P.n_grid;
-    const double v00 = G[a * N + b], v01 = G[a * N + b + 1], v10 = G[(a + 1) * N + b], v11 = G[(a + 1) * N + b + 1];
-    dens[idx] = v00 * (1.0 - tx) * (1.0 - ty) + v01 * (1.0 - tx) * ty + v10 * tx * (1.0 - ty) + v11 * tx * ty;
+    const int b = P.back_idx[2 * i + 1];
+    const double ty = P.back_t[2 * i + 1];
+    const double *row0 = gridT + (long)z * N * N + (long)b * N;
+    const double *row1 = row0 + N;
+    const double *bw = P.back_w + (long)i * N;
+    double acc = 0.0;
+    for (int j = lane; j < N; j += 32) acc += bw[j] * ((1.0 - ty) * row0[j] + ty * row1[j]);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) dens[(long)i * nz + z] = acc;
 }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -225,7 +178,7 @@ size_t hgb_scatter_workspace_bytes(int n_mtot, int n_mrat, int n_redz, int n_gri
     if (n_mtot < 2 || n_mrat < 2 || n_redz < 1 || n_grid < 2) return 0;
     size_t n = (size_t)n_mtot * n_mrat, NN = (size_t)n_grid * n_grid;
     return align256(sizeof(double) * n * n_redz) + align256(sizeof(double) * 2 * n * n_redz) +
-           2 * align256(sizeof(double) * NN * n_redz);
+           align256(sizeof(double) * NN * n_redz);
 }
 
 int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_redz, void *workspace,
@@ -234,8 +187,8 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     const hgb_scatter_plan &P = *plan;
     HGB_CHECK_ARG(P.n_mtot >= 2 && P.n_mrat >= 2 && P.n_grid >= 2 && P.n_levels >= 1);
     HGB_CHECK_ARG(P.pts && P.tri && P.tri_kappa && P.vtx_qinv && P.nbr_ptr && P.nbr_idx && P.nbr_w);
-    HGB_CHECK_ARG(P.level_ptr && P.level_vtx && P.grid_tri && P.grid_bary && P.grid_near && P.weights);
-    HGB_CHECK_ARG(P.back_idx && P.back_t && P.grad_maxiter >= 1);
+    HGB_CHECK_ARG(P.level_ptr && P.level_vtx && P.grid_tri && P.grid_bary && P.grid_near);
+    HGB_CHECK_ARG(P.back_idx && P.back_t && P.back_w && P.grad_maxiter >= 1);
     size_t need = hgb_scatter_workspace_bytes(P.n_mtot, P.n_mrat, n_redz, P.n_grid);
     if (!workspace || workspace_bytes < need) return HGB_ERR_WORKSPACE;
     const size_t n = (size_t)P.n_mtot * P.n_mrat, NN = (size_t)P.n_grid * P.n_grid;
@@ -245,8 +198,6 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     double *grads = (double *)w;
     w += align256(sizeof(double) * 2 * n * n_redz);
     double *gridA = (double *)w;
-    w += align256(sizeof(double) * NN * n_redz);
-    double *gridB = (double *)w;
     cudaStream_t st = (cudaStream_t)stream;
 
     k_gradients<<<n_redz, 256, 0, st>>>(P, dens, n_redz, vals, grads, d_status);
@@ -255,15 +206,8 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     dim3 gct((unsigned)hgb::ceil_div((long)NN, 256), (unsigned)n_redz);
     k_clough_tocher<<<gct, 256, 0, st>>>(P, vals, grads, gridA);
     if ((rc = hgb::check_launch())) return rc;
-    const int N = P.n_grid;
-    dim3 gg((unsigned)hgb::ceil_div(N, 64), (unsigned)hgb::ceil_div(N, 64), (unsigned)n_redz);
-    // along the primary-mass axis: B = W^T A  (utils.py:454-461, einsum "j...,jk...")
-    k_gemm_f64<true><<<gg, 256, 0, st>>>(N, P.weights, 0, gridA, (long)NN, gridB, (long)NN);
-    if ((rc = hgb::check_launch())) return rc;
-    // along the secondary-mass axis: A = B W
-    k_gemm_f64<false><<<gg, 256, 0, st>>>(N, gridB, (long)NN, P.weights, 0, gridA, (long)NN);
-    if ((rc = hgb::check_launch())) return rc;
-    k_back<<<(unsigned)hgb::ceil_div((long)n * n_redz, 256), 256, 0, st>>>(P, gridA, n_redz, dens);
+    const long nwarps = (long)n * n_redz;
+    k_back_dot<<<(unsigned)hgb::ceil_div(nwarps * 32, 256), 256, 0, st>>>(P, gridA, n_redz, dens);
     return hgb::check_launch();
 }
 

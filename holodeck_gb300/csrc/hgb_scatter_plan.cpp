@@ -20,7 +20,9 @@
 //     coordinates (or -1 outside the hull) and the nearest point (greedy descent on the Delaunay
 //     graph, exact for any query point);
 //   * per point: the lower grid cell and fractional offsets of the bilinear interpolation back;
-//   * the Gaussian redistribution matrix W[i][k] = P(bin k | source bin i) of utils.py:382-488.
+//   * the Gaussian redistribution matrix W[i][k] = P(bin k | source bin i) of utils.py:382-488, and
+//     per point the row of (W W) that, combined with the bilinear weights, maps a slice's regular
+//     grid straight to the point's redistributed value.
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
@@ -546,6 +548,30 @@ int hgb_scatter_plan_build(const double *mtot, int n_mtot, const double *mrat, i
         for (int k = 0; k < 2 * N - 1; k++) dm[k] = cdf[k + 1] - cdf[k];
         for (int i = 0; i < N; i++)
             for (int k = 0; k < N; k++) plan->weights[(long)i * N + k] = dm[k - i + N - 1];
+    }
+
+    // The reference redistributes the primary-mass axis twice (see hgb_add_scatter_to_masses):
+    // out[a][b] = sum_j (W W)[j][a] G[j][b].  Sampled bilinearly at point i this is
+    // sum_j bw_i[j] ((1 - ty) G[j][b_i] + ty G[j][b_i + 1]) with the geometry-only row
+    // bw_i[j] = (1 - tx) (W W)[j][a_i] + tx (W W)[j][a_i + 1].
+    {
+        const double *W = plan->weights;
+        std::vector<double> W2((size_t)N * N, 0.0);
+        for (int j = 0; j < N; j++)
+            for (int k = 0; k < N; k++) {
+                double wjk = W[(long)j * N + k];
+                if (wjk == 0.0) continue;
+                const double *wk = W + (long)k * N;
+                double *out = W2.data() + (long)j * N;
+                for (int a = 0; a < N; a++) out[a] += wjk * wk[a];
+            }
+        for (int i = 0; i < n; i++) {
+            int a = plan->back_idx[2 * i];
+            double tx = plan->back_t[2 * i];
+            double *row = plan->back_w + (long)i * N;
+            for (int j = 0; j < N; j++)
+                row[j] = (1.0 - tx) * W2[(long)j * N + a] + tx * W2[(long)j * N + a + 1];
+        }
     }
 
     for (int i = 0; i < n; i++) {

@@ -22,7 +22,7 @@ GRAD_MAXITER = 400     # CloughTocher2DInterpolator default sweep limit
 _DTYPES = dict(pts=np.float64, tri=np.int32, tri_kappa=np.float64, vtx_qinv=np.float64, nbr_ptr=np.int32,
                nbr_idx=np.int32, nbr_w=np.float64, level_ptr=np.int32, level_vtx=np.int32, grid_tri=np.int32,
                grid_bary=np.float64, grid_near=np.int32, grid_axis=np.float64, weights=np.float64,
-               back_idx=np.int32, back_t=np.float64)
+               back_idx=np.int32, back_t=np.float64, back_w=np.float64)
 
 _PLANS = {}
 
@@ -38,7 +38,8 @@ def host_plan(mtot, mrat, scatter, refine=4):
     shapes = dict(pts=(npts, 2), tri=(ntri, 3), tri_kappa=(ntri, 3), vtx_qinv=(npts, 4), nbr_ptr=(npts + 1,),
                   nbr_idx=(nnbr,), nbr_w=(nnbr, 4), level_ptr=(nlev + 1,), level_vtx=(npts,),
                   grid_tri=(ngrid * ngrid,), grid_bary=(ngrid * ngrid, 3), grid_near=(ngrid * ngrid,),
-                  grid_axis=(ngrid,), weights=(ngrid, ngrid), back_idx=(npts, 2), back_t=(npts, 2))
+                  grid_axis=(ngrid,), weights=(ngrid, ngrid), back_idx=(npts, 2), back_t=(npts, 2),
+                  back_w=(npts, ngrid))
     arrs = {kk: np.zeros(shapes[kk], dtype=_DTYPES[kk]) for kk in N._SCATTER_ARRAYS}
     hp = N.HgbScatterHostPlan(**{kk: arrs[kk].ctypes.data_as(ctypes.c_void_p) for kk in N._SCATTER_ARRAYS})
     sz = N.HgbScatterSizes()

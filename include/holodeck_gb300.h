@@ -139,6 +139,7 @@ typedef struct {    /* host arrays, sized by hgb_scatter_plan_bounds */
     double *weights;    /* [n_grid][n_grid] W[source][target] */
     int32_t *back_idx;  /* [n_pts][2] lower grid cell */
     double *back_t;     /* [n_pts][2] fractional offsets */
+    double *back_w;     /* [n_pts][n_grid] (1-tx) (W W)[:, a] + tx (W W)[:, a+1] */
 } hgb_scatter_host_plan;
 
 typedef struct {    /* the same arrays on the device */
@@ -158,6 +159,7 @@ typedef struct {    /* the same arrays on the device */
     const double *weights;
     const int32_t *back_idx;
     const double *back_t;
+    const double *back_w;
     double grad_tol;    /* 1e-6 in the reference */
     int grad_maxiter;   /* 400 in the reference */
 } hgb_scatter_plan;
