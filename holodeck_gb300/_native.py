@@ -16,6 +16,7 @@ HGB_OK = 0
 HGB_ERR_INVALID_ARGUMENT = 1
 HGB_ERR_CUDA = 2
 HGB_ERR_WORKSPACE = 3
+HGB_ERR_CAPACITY = 4
 
 STATUS_ITERATION_LIMIT = 1
 STATUS_INVALID_REDSHIFT = 2
@@ -101,6 +102,7 @@ SIGNATURES = [
                                    _p, _p, _p, _p]),
     ("hgb_sort_workspace_bytes", _sz, [_l]),
     ("hgb_argsort_f0_desc", _i, [_p, _l, _i, _p, _p, _sz, _p]),
+    ("hgb_argsort_f0_desc_static", _i, [_p, _l, _i, _p, _p]),
     ("hgb_loudest_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
     ("hgb_loudest_hc_from_sorted", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p]),
     ("hgb_sam_poisson_gwb_workspace_bytes", _sz, [_l, _i, _i]),

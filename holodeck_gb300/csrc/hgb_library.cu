@@ -52,6 +52,7 @@ const char *hgb_error_string(int code) {
         case HGB_ERR_INVALID_ARGUMENT: return "invalid argument";
         case HGB_ERR_CUDA: return "CUDA error";
         case HGB_ERR_WORKSPACE: return "workspace too small";
+        case HGB_ERR_CAPACITY: return "input exceeds the static scratch capacity";
         default: return "unknown error";
     }
 }

@@ -32,6 +32,7 @@ extern "C" {
 #define HGB_ERR_INVALID_ARGUMENT 1
 #define HGB_ERR_CUDA 2
 #define HGB_ERR_WORKSPACE 3
+#define HGB_ERR_CAPACITY 4   /* input larger than a static scratch array holds */
 
 /* ---- device status bits (OR-ed into *d_status) */
 #define HGB_STATUS_ITERATION_LIMIT 1   /* a bounded sampling / root-finding loop ran out */
@@ -229,6 +230,18 @@ int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mt
 size_t hgb_sort_workspace_bytes(long n_bins);
 int hgb_argsort_f0_desc(const double *h2fdf, long n_bins, int n_freq, int32_t *order,
                         void *workspace, size_t workspace_bytes, void *stream);
+
+/* No reference counterpart.  Allocation-free variant of hgb_argsort_f0_desc for callers that
+ * cannot supply a workspace: same arguments without workspace/workspace_bytes, same `order`.
+ * Its scratch is a file-scope device array of HGB_SORT_STATIC_BYTES (24 MiB) per device, so
+ * n_bins <= HGB_SORT_STATIC_MAX_BINS (2^20); larger inputs return HGB_ERR_CAPACITY with nothing
+ * enqueued.  The first call on each device (with that device current) looks the array up with
+ * cudaGetSymbolAddress, which loads the module: make that first call before any stream capture.
+ * Every call on a device shares the one array, so calls that overlap in time (different streams
+ * or host threads) race; the caller serialises them. */
+#define HGB_SORT_STATIC_MAX_BINS 1048576L
+#define HGB_SORT_STATIC_BYTES (24UL << 20)
+int hgb_argsort_f0_desc_static(const double *h2fdf, long n_bins, int n_freq, int32_t *order, void *stream);
 
 /* Poisson realizations with the loudest-L split.  Replaces cyutils.loudest_hc_from_sorted,
  * cyutils.pyx:1220-1344: for every realization r and frequency f the bins are visited in
