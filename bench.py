@@ -101,11 +101,6 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def kernel_event_timer(torch):
-    """Times the realization kernel on its launching stream with CUDA events (torch's current stream)."""
-    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -182,19 +177,24 @@ def run_gpu(args):
     order = single_sources.sort_order_device(h2fdf)
     from holodeck_gb300 import cyutils
     nb = int(number.numel() // NFREQ)
+    lib = N.load()
+    N.check(lib.hgb_bulk_timing(1), "hgb_bulk_timing")
     times = []
     for i in range(3):
         flush.zero_()
-        e0, e1 = kernel_event_timer(torch)
-        e0.record()
         cyutils.loudest_device(number.reshape(-1, NFREQ), h2fdf.reshape(-1, NFREQ), NREALS, NLOUD, order, seed=i)
-        e1.record()
         torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1) / 1e3)
-    t_real = min(times)
+        times.append(float(lib.hgb_bulk_last_ms()) / 1e3)
+    N.check(lib.hgb_bulk_timing(0), "hgb_bulk_timing")
+    t_real = sum(times) / len(times)
     draws = nb * NFREQ * NREALS
-    # algorithmic bytes of one launch: read number + h2fdf (gathered once), write hc2ss + hc2bg
-    alg_bytes = 2 * 8 * nb * NFREQ * 2 + 8 * NFREQ * NREALS * (NLOUD + 1)
+    # algorithmic bytes of one k_bulk launch, per realization group: every bin's expectation and the
+    # strain of the bins with a nonzero expectation (8 B each), each realization's first bulk
+    # position read, the per-chunk partials written
+    n_rgroups = -(-NREALS // 1024)
+    nchunk = max(1, -(-152 * 5 * 2 // (NFREQ * n_rgroups)))
+    n_pos = int((number > 0).sum().item())
+    alg_bytes = (8 * nb * NFREQ + 8 * n_pos) * n_rgroups + 4 * NFREQ * NREALS + 8 * nchunk * NFREQ * NREALS
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -206,7 +206,7 @@ def run_gpu(args):
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
-            traffic = json.load(fh).get("k_loudest_philox_bytes_per_launch")
+            traffic = json.load(fh).get("k_bulk_bytes_per_launch")
     except (OSError, ValueError):
         pass
 
@@ -224,7 +224,7 @@ def run_gpu(args):
             "e2e": {"value": world * NREALS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"kernel": "k_loudest_philox", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
+            "roofline": {"kernel": "k_bulk", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "launch_s": t_real, "draws_per_s": draws / t_real,
                          "note": "issue-bound sampler: HBM fraction shown for the contract, see profiles/"},
@@ -338,6 +338,21 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_profile(args):
+    """One model evaluation of the bench workload with ``--nfreqs`` frequencies, no timing: the
+    program the ncu captures run (a smaller frequency count keeps a full capture short)."""
+    import torch
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    _, fe = H.utils.pta_freqs(16.0 * C.YR, NFREQ)
+    fe = fe[:args.nfreqs + 1]
+    for i in range(args.warmup + 1):
+        sam, hard = make_model(H, C)
+        sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=i, return_torch=True)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -345,8 +360,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="run warmup + 1 untimed evaluations (for ncu)")
+    ap.add_argument("--nfreqs", type=int, default=NFREQ, help="frequencies of a --profile run")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

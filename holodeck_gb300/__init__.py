@@ -17,5 +17,6 @@ from . import utils  # noqa: E402
 from . import host_relations, hardening  # noqa: E402
 from . import cyutils, gravwaves, single_sources  # noqa: E402
 from . import sams  # noqa: E402
+from . import librarian  # noqa: E402
 
 __version__ = "0.1.0"

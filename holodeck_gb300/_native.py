@@ -65,7 +65,8 @@ class HgbScatterSizes(ctypes.Structure):
 
 
 _SCATTER_ARRAYS = ["pts", "tri", "tri_kappa", "vtx_qinv", "nbr_ptr", "nbr_idx", "nbr_w", "level_ptr", "level_vtx",
-                   "grid_tri", "grid_bary", "grid_near", "grid_axis", "weights", "back_idx", "back_t", "back_w"]
+                   "grid_tri", "grid_bary", "grid_near", "grid_axis", "weights", "back_idx", "back_t", "back_w",
+                   "lv_nbr_ptr", "lv_nbr", "lv_nbr_w", "lv_qinv"]
 
 
 class HgbScatterHostPlan(ctypes.Structure):
@@ -105,6 +106,14 @@ SIGNATURES = [
     ("hgb_argsort_f0_desc_static", _i, [_p, _l, _i, _p, _p]),
     ("hgb_loudest_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
     ("hgb_loudest_hc_from_sorted", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p]),
+    ("hgb_param_grids", _i, [_p, _i, _i, _i, _p, _i, _p, _d, ctypes.POINTER(HgbCosmo), _p, _p, _p, _p, _p, _p,
+                             _p]),
+    ("hgb_loudest_par_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
+    ("hgb_loudest_hc_and_par_from_sorted", _i, [_p, _p, _i, _i, _i, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _p,
+                                                _p, _p, _p, _p, _p, _p, _p, _p, _p, _sz, _p, _p]),
+    ("hgb_model_details", _i, [_p, _p, _p, _p, _i, _i, _i, _i] + [_p] * 12),
+    ("hgb_bulk_timing", _i, [_i]),
+    ("hgb_bulk_last_ms", ctypes.c_float, []),
     ("hgb_sam_poisson_gwb_workspace_bytes", _sz, [_l, _i, _i]),
     ("hgb_sam_poisson_gwb", _i, [_p, _p, _l, _i, _i, _i, _u64, _p, _p, _p, _sz, _p, _p]),
 ]
@@ -160,7 +169,8 @@ KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
-    "hgb_loudest_hc_from_sorted": 3, "hgb_sam_poisson_gwb": 2,
+    "hgb_loudest_hc_from_sorted": 6, "hgb_sam_poisson_gwb": 2, "hgb_param_grids": 1, "hgb_model_details": 9,
+    "hgb_loudest_hc_and_par_from_sorted": 6,
 }
 _launches = [0]
 

@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libholodeck_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NO_FMA = {"hgb_density.cu", "hgb_hardening.cu", "hgb_strain.cu", "hgb_scatter.cu"}
+NO_FMA = {"hgb_density.cu", "hgb_hardening.cu", "hgb_strain.cu", "hgb_scatter.cu", "hgb_details.cu"}
 
 
 def nvcc():

@@ -5,7 +5,8 @@
 //    two phases: k_dbn_2pwl walks the separation steps (one block per (mtot, mrat) cell, one thread
 //    per starting redshift, step tables in shared memory) and records, per target frequency, the
 //    interpolated time of the bracketing step; k_dbn_2pwl_eval then evaluates redshift, distance,
-//    residence time and number for every bracketed (redz, frequency) element in parallel.
+//    residence time and number for every bracketed (redz, frequency) element in parallel, with the
+//    model's (half-)integer exponents taken as products and square roots instead of pow().
 //  * hgb_dbn_gw: differential binary number for Hard_GW (sam_cyutils.pyx:788-899); one thread per
 //    grid point.
 // FP64 throughout (the hardening integral and the lookback-time -> redshift inversion are the
@@ -166,10 +167,37 @@ __global__ void k_hardening_norm(CyConst cc, NormArgs a, const double *__restric
 // differential binary number, Fixed_Time_2PL_SAM
 // ------------------------------------------------------------------------------------------------
 
+// x^y for an exponent fixed per call.  Integer and half-integer exponents up to |y| = 8.5 (the
+// hardening model's defaults give -3.5 and -2) are evaluated as products and one square root,
+// within a few ulp of pow(); any other exponent goes to pow().
+struct PowPlan {
+    int kind;   // 0: pow(), 1: integer, 2: half-integer
+    int n;      // |y| rounded down
+    int neg;    // y < 0
+};
+
+PowPlan pow_plan(double y) {
+    PowPlan p{0, 0, y < 0.0};
+    const double ay = fabs(y), twice = 2.0 * ay;
+    if (ay <= 8.5 && twice == floor(twice)) {
+        p.n = (int)floor(ay);
+        p.kind = (ay == floor(ay)) ? 1 : 2;
+    }
+    return p;
+}
+
+__device__ __forceinline__ double pow_planned(double x, double y, PowPlan p) {
+    if (p.kind == 0) return pow(x, y);
+    double r = (p.kind == 2) ? sqrt(x) : 1.0;
+    for (int i = 0; i < p.n; i++) r *= x;
+    return p.neg ? 1.0 / r : r;
+}
+
 struct Dbn2plArgs {
     double sepa_init_log10, rchar, gi, go;
     int num_steps, n_freq, fobs_sorted;
     int n_mtot, n_mrat, n_redz, n_interp;
+    PowPlan p_outer, p_inner;   // exponents -go + gi and gi - 1 of the hardening rate
 };
 
 __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ fobs,
@@ -373,9 +401,10 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
         double new_redz = hgb::interp_between(new_time, ag[ni], ag[ni + 1], zg[ni], zg[ni + 1]);
         double dcom = hgb::interp_between(new_time, ag[ni], ag[ni + 1], dg[ni], dg[ni + 1]);
         double target_frst_orb = ft[f] * (1.0 + new_redz);
-        double sp = cc.ksepa * mt13 / pow(target_frst_orb, 2.0 / 3.0);
+        const double cb = cbrt(target_frst_orb);   // target^(2/3) as cbrt(target)^2
+        double sp = cc.ksepa * mt13 / (cb * cb);
         double xx = sp / a.rchar;
-        double dadt = -norm * pow(1.0 + xx, -a.go + a.gi) / pow(xx, a.gi - 1.0);
+        double dadt = -norm * pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
         dadt += cc.c_dadt * mt3 * mr / (sp * sp * sp) / mr12;
         double tres = -(2.0 / 3.0) * sp / dadt;
         double dcm = dcom / HGB_CY_MPC;
@@ -429,6 +458,198 @@ __global__ void k_dbn_gw(CyConst cc, const double *__restrict__ fobs, int NF, co
     }
 }
 
+// The same root, sixteen cells per block (one warp each) in lock step.  The node constants live in
+// registers (node s = lane + 32 k), the trapezoid terms of all sixteen cells go to shared memory,
+// and one warp forms the sixteen ordered sums with one lane per cell, so the step-order summation
+// costs a sixteenth of a warp instruction per step and cell instead of one.  Arithmetic and
+// evaluation sequence are those of warp_lifetime / warp_brent.
+constexpr int NB_CELLS = 16;
+constexpr int NB_NODES = 10;   // nodes per lane: nsteps + 1 <= 320
+
+__global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst cc, NormArgs a,
+                                                                       const double *__restrict__ mtot,
+                                                                       const double *__restrict__ mrat, int n,
+                                                                       double *__restrict__ norm_log10,
+                                                                       double *__restrict__ norm, int *d_status) {
+    extern __shared__ double smem[];
+    __shared__ double s_time[NB_CELLS];
+    __shared__ int s_active[NB_CELLS];
+    const int S = a.nsteps;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * NB_CELLS + warp;
+    const bool valid = cell < n;
+    double *dts = smem;                                  // [NB_CELLS][S]
+    double *crow = smem + (size_t)NB_CELLS * S;          // [NB_CELLS][S + 1]: log10 separations, then c[s]
+    double *myc = crow + (size_t)warp * (S + 1);
+    double *mydt = dts + (size_t)warp * S;
+    const double mt = valid ? mtot[cell] : 1.0, mr = valid ? mrat[cell] : 1.0;
+    // log10 separation nodes by repeated subtraction (sam_cyutils.pyx:367-383), one lane per cell
+    if (warp == 0 && lane < NB_CELLS) {
+        const int c = blockIdx.x * NB_CELLS + lane;
+        if (c < n) {
+            double *row = crow + (size_t)lane * (S + 1);
+            const double risco_log10 = log10(3.0 * HGB_CY_SCHW * mtot[c]);
+            const double dx = (a.sepa_init_log10 - risco_log10) / S;
+            double sl = a.sepa_init_log10;
+            row[0] = sl;
+            for (int s = 1; s <= S; s++) {
+                sl -= dx;
+                row[s] = sl;
+            }
+        }
+    }
+    __syncthreads();
+    double aa[NB_NODES], bb[NB_NODES], gw[NB_NODES], sp[NB_NODES];
+#pragma unroll
+    for (int k = 0; k < NB_NODES; k++) {
+        const int s = lane + 32 * k;
+        aa[k] = bb[k] = 1.0;
+        gw[k] = sp[k] = 0.0;
+        if (valid && s <= S) {
+            const double x = pow(10.0, myc[s]);
+            const double xx = x / a.rchar;
+            aa[k] = pow(1.0 + xx, -a.go + a.gi);
+            bb[k] = pow(xx, a.gi - 1.0);
+            gw[k] = hgb::hard_gw(cc.c_dadt, mt, mr, x);
+            sp[k] = x;
+        }
+    }
+    __syncwarp();
+    // c[s] = 2 (sepa[s+1] - sepa[s]), s < S (overwrites this warp's log10 row)
+#pragma unroll
+    for (int k = 0; k < NB_NODES; k++) {
+        double nxt = __shfl_down_sync(0xffffffffu, sp[k], 1);
+        const double wrap = __shfl_sync(0xffffffffu, (k + 1 < NB_NODES) ? sp[k + 1] : 0.0, 0);
+        if (lane == 31) nxt = wrap;
+        const int s = lane + 32 * k;
+        if (valid && s < S) myc[s] = 2.0 * (nxt - sp[k]);
+    }
+    __syncthreads();
+
+    // Brent's method as in warp_brent, one evaluation per round for every unfinished cell
+    double xa = NORM_LOG10_LO, xb = NORM_LOG10_HI, xc = 0.0, fa = 0.0, fb = 0.0, fc = 0.0, d = 0.0, e = 0.0;
+    int stage = 0, it = 0, nit = 0;
+    bool done = !valid;
+    double root = 0.0;
+    for (int round = 0; round < BRENT_MAXITER + 2; round++) {
+        const double xe = (stage == 0) ? xa : xb;
+        if (!done) {
+            const double nrm = pow(10.0, xe);
+            double v[NB_NODES];
+#pragma unroll
+            for (int k = 0; k < NB_NODES; k++) {
+                double dl = -nrm * aa[k] / bb[k];
+                dl += gw[k];
+                v[k] = dl;
+            }
+#pragma unroll
+            for (int k = 0; k < NB_NODES; k++) {
+                double vn = __shfl_down_sync(0xffffffffu, v[k], 1);
+                const double wrap = __shfl_sync(0xffffffffu, (k + 1 < NB_NODES) ? v[k + 1] : 0.0, 0);
+                if (lane == 31) vn = wrap;
+                const int s = lane + 32 * k;
+                if (s < S) mydt[s] = myc[s] / (v[k] + vn);
+            }
+        }
+        if (lane == 0) s_active[warp] = done ? 0 : 1;
+        __syncthreads();
+        if (warp == 0 && lane < NB_CELLS && s_active[lane]) {
+            const double *row = dts + (size_t)lane * S;
+            double time = 0.0;
+            for (int s = 0; s < S; s++) time += row[s];
+            s_time[lane] = time;
+        }
+        __syncthreads();
+        if (done) continue;
+        const double fv = s_time[warp] - a.target_time;
+        if (stage == 0) {
+            fa = fv;
+            stage = 1;
+            continue;
+        }
+        fb = fv;
+        if (stage == 1) {
+            stage = 2;
+            if (fa * fb > 0.0) {
+                root = 0.0;
+                done = true;
+                continue;
+            }
+            if (fa == 0.0) {
+                root = xa;
+                done = true;
+                continue;
+            }
+            if (fb == 0.0) {
+                root = xb;
+                done = true;
+                continue;
+            }
+            xc = xa;
+            fc = fa;
+            d = xb - xa;
+            e = d;
+            it = 0;
+        } else {
+            it++;
+            if (it >= BRENT_MAXITER) {
+                root = xb;
+                nit = BRENT_MAXITER + 1;
+                done = true;
+                continue;
+            }
+        }
+        nit = it + 1;
+        if (fb * fc > 0.0) {
+            xc = xa;
+            fc = fa;
+            d = xb - xa;
+            e = d;
+        }
+        if (fabs(fc) < fabs(fb)) {
+            xa = xb; xb = xc; xc = xa;
+            fa = fb; fb = fc; fc = fa;
+        }
+        const double tol = 0.5 * (BRENT_XTOL + BRENT_RTOL * fabs(xb));
+        const double m = 0.5 * (xc - xb);
+        if (fb == 0.0 || fabs(m) < tol) {
+            root = xb;
+            done = true;
+            continue;
+        }
+        if (fabs(e) > tol && fabs(fb) < fabs(fa)) {
+            double sst;
+            if (xa == xc) {
+                sst = -fb * (xb - xa) / (fb - fa);
+            } else {
+                const double da = (fa - fb) / (xa - xb);
+                const double dc = (fc - fb) / (xc - xb);
+                sst = -fb * (fc * dc - fa * da) / (dc * da * (fc - fa));
+            }
+            if (2.0 * fabs(sst) < fmin(fabs(e), 3.0 * fabs(m) - tol)) {
+                e = d;
+                d = sst;
+            } else {
+                d = m;
+                e = m;
+            }
+        } else {
+            d = m;
+            e = m;
+        }
+        xa = xb;
+        fa = fb;
+        xb = xb + ((fabs(d) > tol) ? d : ((m > 0.0) ? tol : -tol));
+    }
+    if (valid && lane == 0) {
+        norm_log10[cell] = root;
+        if (norm) norm[cell] = pow(10.0, root);
+        if (nit > BRENT_MAXITER) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+    }
+}
+
+size_t norm_blk_smem(int nsteps) { return sizeof(double) * (size_t)NB_CELLS * (2 * (size_t)nsteps + 1); }
+
 size_t norm_smem_per_warp(int nsteps) { return (size_t)5 * (nsteps + 1) * sizeof(double); }
 
 }  // namespace
@@ -456,6 +677,18 @@ int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const d
         }
     }
     NormArgs a{target_time, log10(sepa_init), rchar, gamma_inner, gamma_outer, nsteps};
+    if (nsteps + 1 <= 32 * NB_NODES) {
+        const size_t bsmem = norm_blk_smem(nsteps);
+        cudaError_t err = cudaFuncSetAttribute(k_hardening_norm_blk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)bsmem);
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+        k_hardening_norm_blk<<<(unsigned)hgb::ceil_div(n, NB_CELLS), NB_CELLS * 32, bsmem, (cudaStream_t)stream>>>(
+            hgb::cy_const(), a, mtot, mrat, n, norm_log10, norm, d_status);
+        return hgb::check_launch();
+    }
     unsigned blocks = (unsigned)hgb::ceil_div(n, wpb);
     k_hardening_norm<<<blocks, 32 * wpb, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, mtot, mrat, n,
                                                                        norm_log10, norm, d_status);
@@ -473,7 +706,8 @@ int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sep
     HGB_CHECK_ARG(cosmo->grid_size >= 2 && cosmo->grid_z && cosmo->grid_age && cosmo->grid_dcom);
     HGB_CHECK_ARG(sepa_init > 0.0 && rchar > 0.0);
     Dbn2plArgs a{log10(sepa_init), rchar, gamma_inner, gamma_outer, num_steps, n_freq, fobs_sorted ? 1 : 0,
-                 n_mtot, n_mrat, n_redz, cosmo->grid_size};
+                 n_mtot, n_mrat, n_redz, cosmo->grid_size, pow_plan(-gamma_outer + gamma_inner),
+                 pow_plan(gamma_inner - 1.0)};
     size_t smem = sizeof(double) * ((size_t)3 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
                                     2 * (size_t)num_steps);
     HGB_CHECK_ARG(smem <= 200 * 1024);

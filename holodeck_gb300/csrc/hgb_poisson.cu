@@ -3,32 +3,50 @@
 // Replaces cyutils.loudest_hc_from_sorted (holodeck/cyutils.pyx:1220-1344) and
 // cyutils.sam_poisson_gwb (holodeck/cyutils.pyx:854-897).
 //
-// Layout: the (B, F) number and h2fdf grids are gathered once into loudest-first order and
-// transposed to (F, B), so one frequency's sorted bins are contiguous.  A block owns one
-// frequency, up to RB*RPT realizations (RPT per thread, kept in shared memory) and one chunk of
-// bins; a chunk is every nchunk-th tile of RB sorted bins, so chunks carry the same mix of cheap
-// and expensive bins and finish together.  The block stages a tile in shared memory with its
-// per-bin sampler constants -- computed once per bin per block, i.e. amortised over all
-// realizations -- and each thread walks the tile in sorted order for its realizations.  All
-// threads of a warp see the same bin, so the choice of sampler is warp-uniform and bins with zero
-// expectation (most of the grid) cost one shared-memory load per thread.
+// The reference visits, for every realization r and frequency f, all bins in loudest-first order,
+// draws n ~ Poisson(number), hands the first L sources to the loudest slots and adds the rest,
+// n * h2fdf, to the background.  Only the first L sources depend on the visiting order; the
+// background is an order-free sum.  The GPU path splits the walk accordingly:
+//
+//   1. k_gather_sorted   number / h2fdf gathered into loudest-first (F, B) order.
+//   2. k_cum_sum/write   per frequency, the cumulative expectation C[k] = sum_{k' < k} number[k']
+//                        along that order (FP64), in segments.
+//   3. k_loud_prefix     one thread per (f, r) fills the L slots exactly in order, jumping from one
+//                        occupied bin to the next: with i the first unvisited bin and E ~ Exp(1),
+//                        the next bin with n >= 1 is the smallest j >= i with C[j+1] - C[i] > E
+//                        (P(no source in bins i..j-1) = exp(-(C[j] - C[i]))), and its count is
+//                        zero-truncated Poisson.  So the loudest slots cost ~L events instead of a
+//                        walk over the tens of thousands of bins that precede them.  The bin that
+//                        fills the last slot adds its remaining sources to the background, and
+//                        Q[f, r], the first bin not yet visited, is recorded.
+//   4. k_bulk            the background of every bin at sorted position >= Q[f, r]: a block owns
+//                        one frequency, RB * RPT realizations and one chunk of bins (every
+//                        nchunk-th tile of RB bins, so chunks carry the same mix and finish
+//                        together), stages a tile's per-bin sampler constants in shared memory --
+//                        computed once per bin, amortised over all realizations -- sorts the tile's
+//                        bins into one list per sampler kind, and runs each list as a tight loop in
+//                        which every lane draws for its own realizations.
+//   5. k_bg_reduce       per (f, r): prefix remainder + the chunks' partial sums, in fixed order.
+// sam_poisson_gwb is step 4 with Q = 0 over the bins in grid order, then step 5.
 //
 // Draws (HGB_RNG_PHILOX): counter-based Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) keyed by
-// the 64-bit seed; counters are built from (sorted bin, realization, frequency, stream word), so
-// results do not depend on chunking.  Samplers by expectation lambda:
+// the 64-bit seed; counters are built from (sorted bin or event index, realization, frequency,
+// draw family), so results do not depend on the chunking.  Bulk samplers by expectation lambda:
 //   lambda <= 0 or NaN        n = 0, no draw
-//   lambda < TINY             geometric skipping over a thread's realizations: the gap to the next
-//                             realization with n >= 1 is floor(-ln u / lambda) (P(n = 0) = e^-lambda),
-//                             so one 64-bit uniform usually settles all RPT realizations; a hit
-//                             draws n from the zero-truncated Poisson
-//   TINY <= lambda < 10       inversion of a 64-bit uniform against a per-bin table of
-//                             floor(CDF(n) 2^64) (n = 0) and floor(CDF(n) 2^32) (n >= 1); two
+//   lambda < TINY             geometric skipping over a lane's realizations: the gap to the next
+//                             realization with n >= 1 is floor(-ln u / lambda), so one 64-bit
+//                             uniform usually settles all RPT realizations; a hit draws n from the
+//                             zero-truncated Poisson
+//   TINY <= lambda < 10       inversion of a 32-bit uniform against the bin's table of
+//                             floor(CDF(n) 2^32), n < 32, by a branch-free binary search; four
 //                             realizations per Philox call
 //   10 <= lambda < 2^22       PTRS, transformed rejection with squeeze (Hormann 1993, Insurance:
-//                             Mathematics and Economics 12, 39-45) in FP32, acceptance test in the
-//                             log-pmf form of Loader's saddle-point expansion (bd0 + Stirling
-//                             remainder), so nothing cancels in FP32; two realizations' first
-//                             attempts per Philox call
+//                             Mathematics and Economics 12, 39-45) in FP32: the acceptance test uses
+//                             the log-pmf in Loader's saddle-point form (bd0 + Stirling remainder,
+//                             Loader 2000), so nothing cancels in FP32.  Each lane runs one loop
+//                             over its realizations that consumes two attempts per Philox call and
+//                             moves to the next realization on acceptance, so a rejection delays
+//                             only its own lane by one attempt
 //   2^22 <= lambda <= 1e10    PTRS in FP64
 //   lambda > 1e10             Normal(lambda, sqrt(lambda)) by Box-Muller, as the reference does
 // Counts are integers; background sums accumulate n * h2fdf * 2^100 in FP32 with Kahan
@@ -46,38 +64,65 @@
 namespace {
 
 constexpr int RB = 128;                  // threads per block == bins per staged tile
+constexpr int NWARP = RB / 32;
 constexpr int RPT = 8;                   // realizations per thread
-constexpr int NT = 24;                   // CDF thresholds per small-lambda bin
+static_assert(RPT % 4 == 0, "the table passes draw four realizations per Philox call");
+constexpr int NT = 32;                   // CDF thresholds per small-lambda bin
 constexpr double TINY = 0.02;            // geometric skipping below this expectation
 constexpr double NORMAL_THRESH = 1e10;   // long(1e10) in cyutils.pyx:1223
 constexpr double PTRS_MIN = 10.0;
 constexpr double PTRS32_MAX = 4194304.0; // 2^22: k stays exact in FP32
 constexpr int MAX_ATTEMPTS = 64;
+constexpr int MAX_PTRS_ITERS = 2 * RPT + 64;   // attempts of one lane over its RPT realizations
 constexpr int MAX_INVERSION = 4096;
-// stream words (counter .w) of the different draw families
-constexpr uint32_t W_PAIR = 0u;             // first draw / first PTRS attempt of a realization pair
-constexpr uint32_t W_RETRY = 0x10000000u;   // | attempt: further PTRS attempts of one realization
-constexpr uint32_t W_SKIP = 0x20000000u;    // | step: geometric skipping of a thread's realizations
-constexpr uint32_t W_WIDE = 0x30000000u;    // | attempt: PTRS64 / Normal draws
+constexpr int MAX_PREFIX_EXTRA = 1024;   // prefix events beyond L (Normal draws below 1)
+constexpr double TABLE_MAX = 65536.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 9
+constexpr int TMAX = 4096;               // table entries (>= 14 * 256 + 9)
+constexpr int ARENA_WORDS = TMAX + TMAX / 2;   // one largest table: cdf words + u16 guide cells
+constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
+constexpr int TABLE_WARP_MAX = 1024;     // larger tables are built by the whole block
+constexpr float TABLE_SIGMAS = 7.0f;     // the table covers lambda +- 7 sqrt(lambda) (tails < 1e-11)
+// draw families (counter .w high bits)
+constexpr uint32_t W_SMALL = 0x00000000u;   // | call: 4 realizations per call
+constexpr uint32_t W_PTRS = 0x10000000u;    // | iteration / 2
+constexpr uint32_t W_TABLE = 0x50000000u;   // | call: 4 realizations per call
+constexpr uint32_t W_SKIP = 0x20000000u;    // | step: geometric skipping of a lane's realizations
+constexpr uint32_t W_WIDE = 0x30000000u;    // | slot << 8 | attempt: PTRS64 / Normal draws
+constexpr uint32_t W_PREFIX = 0x40000000u;  // | attempt: prefix events (counter .z = event index)
 constexpr uint32_t DOMAIN_GWB = 0x80000000u;
 constexpr float HSCALE = 0x1.0p100f;     // keeps h2fdf (1e-30 .. 1e-20) far from FP32 subnormals
 constexpr double HSCALE_INV = 0x1.0p-100;
 
 enum BinKind : int {
-    KIND_NONE = 0, KIND_TINY = 1, KIND_SMALL = 2, KIND_PTRS32 = 3, KIND_PTRS64 = 4, KIND_NORMAL = 5
+    KIND_NONE = 0, KIND_TINY = 1, KIND_SMALL = 2, KIND_TABLE = 3, KIND_PTRS32 = 4, KIND_WIDE = 5, NKIND = 6
 };
 
-// ---- Philox4x32-10
+// ---- Philox4x32-10 with the ten round keys precomputed (they live in the kernel's parameter space)
 constexpr uint32_t PH_M0 = 0xD2511F53u, PH_M1 = 0xCD9E8D57u, PH_W0 = 0x9E3779B9u, PH_W1 = 0xBB67AE85u;
 
-__device__ __forceinline__ uint4 philox(uint4 c, uint2 k) {
+struct PhiloxKey {
+    uint32_t k0[10], k1[10];
+};
+
+PhiloxKey make_key(uint64_t seed) {
+    PhiloxKey K;
+    uint32_t a = (uint32_t)seed, b = (uint32_t)(seed >> 32);
+    for (int i = 0; i < 10; i++) {
+        K.k0[i] = a;
+        K.k1[i] = b;
+        a += PH_W0;
+        b += PH_W1;
+    }
+    return K;
+}
+
+__device__ __forceinline__ uint4 philox(uint4 c, const PhiloxKey &K) {
 #pragma unroll
     for (int i = 0; i < 10; i++) {
-        uint32_t hi0 = __umulhi(PH_M0, c.x), lo0 = PH_M0 * c.x;
-        uint32_t hi1 = __umulhi(PH_M1, c.z), lo1 = PH_M1 * c.z;
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-        k.x += PH_W0;
-        k.y += PH_W1;
+        const uint64_t p0 = (uint64_t)PH_M0 * c.x;
+        const uint64_t p1 = (uint64_t)PH_M1 * c.z;
+        c = make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ K.k0[i], (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ K.k1[i],
+                       (uint32_t)p0);
     }
     return c;
 }
@@ -91,150 +136,185 @@ __device__ __forceinline__ unsigned long long w64(uint32_t hi, uint32_t lo) {
 }
 
 // log(k!) for k < 16, used by the PTRS acceptance test in the far lower tail
-__constant__ double c_lgam[16] = {
-    0.0, 0.0, 0.69314718055994531, 1.791759469228055, 3.1780538303479458, 4.7874917427820458,
-    6.5792512120101012, 8.5251613610654147, 10.604602902745251, 12.801827480081469, 15.104412573075516,
-    17.502307845873887, 19.987214495661885, 22.552163853123425, 25.19122118273868, 27.89927138384089};
-// 1/n for the CDF recursion p(n) = p(n-1) lambda / n
-__constant__ double c_inv[NT] = {
-    0.0, 1.0, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8, 1.0 / 9, 1.0 / 10, 1.0 / 11,
-    1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20, 1.0 / 21, 1.0 / 22,
-    1.0 / 23};
+__constant__ float c_lgam[16] = {
+    0.0f, 0.0f, 0.69314718055994531f, 1.791759469228055f, 3.1780538303479458f, 4.7874917427820458f,
+    6.5792512120101012f, 8.5251613610654147f, 10.604602902745251f, 12.801827480081469f, 15.104412573075516f,
+    17.502307845873887f, 19.987214495661885f, 22.552163853123425f, 25.19122118273868f, 27.89927138384089f};
 
-// Per-bin sampler constants of one staged tile, shared by every realization of the block.
+// Stirling-series remainder stirlerr(n) = log(n!) - (n + 1/2) log n + n - log(2 pi)/2, n < 16
+// (evaluated from the definition in float64); larger n use the asymptotic series.
+__constant__ float c_stirl[16] = {
+    0.000000000e+00f, 8.106146680e-02f, 4.134069596e-02f, 2.767792568e-02f, 2.079067210e-02f, 1.664469119e-02f,
+    1.387612882e-02f, 1.189670995e-02f, 1.041126526e-02f, 9.255462183e-03f, 8.330563433e-03f, 7.573675488e-03f,
+    6.942840107e-03f, 6.408994188e-03f, 5.951370113e-03f, 5.554733552e-03f};
+// 1/n for the small-lambda CDF recursion p(n) = p(n-1) lambda / n
+__constant__ float c_invf[NT] = {
+    0.0f, 1.0f, 1.0f / 2, 1.0f / 3, 1.0f / 4, 1.0f / 5, 1.0f / 6, 1.0f / 7, 1.0f / 8, 1.0f / 9, 1.0f / 10,
+    1.0f / 11, 1.0f / 12, 1.0f / 13, 1.0f / 14, 1.0f / 15, 1.0f / 16, 1.0f / 17, 1.0f / 18, 1.0f / 19, 1.0f / 20,
+    1.0f / 21, 1.0f / 22, 1.0f / 23, 1.0f / 24, 1.0f / 25, 1.0f / 26, 1.0f / 27, 1.0f / 28, 1.0f / 29, 1.0f / 30,
+    1.0f / 31};
+
+// Per-bin sampler constants of one staged tile, shared by every realization of the block.  The
+// small-lambda thresholds and the table of the current table-kind bin share one region: the
+// small-lambda pass finishes before the first table is built.
 struct Tile {
-    unsigned long long t0[RB];        // floor(e^-lambda 2^64): u < t0 <=> n = 0
+    union {
+        unsigned int thr[NT][RB];                 // small lambda: floor(CDF(n) 2^32), n = 0..31
+        unsigned int arena[ARENA_WORDS];          // table kind: packed cdf (u32) + guide (u16) tables
+    } u;
     unsigned long long tskip[RB];     // tiny lambda: floor(e^(-RPT lambda) 2^64): no hit in RPT draws
-    unsigned int thr[NT][RB];         // small lambda: floor(CDF(n) 2^32), n >= 1 (row 0 unused)
+    unsigned long long scan[NWARP];
     double lam[RB];
-    double h[RB];                     // exact h2fdf (for the loudest slots)
     float hs[RB];                     // h2fdf * 2^100 (for the background sums)
-    float b[RB], a[RB], vr[RB], log_inva[RB], frac43[RB], lamf[RB];
+    float b[RB], a[RB], vr[RB], log_inva[RB], frac[RB], lamf[RB], loglam[RB];
     int lam_int[RB];
-    int kind[RB];
+    int tb_klo[RB], tb_S[RB], tb_gb[RB];   // table kind: first count, entries, log2 guide cells
+    int pos[RB];                      // sorted position (loudest) or grid index (gwb) of the bin
+    unsigned char list[NKIND][RB];    // tile-local bin indices per kind, in bin order
+    int wcount[NWARP][NKIND];
+    float lgam[16];
 };
 
-__device__ __forceinline__ unsigned long long sat64(double p) {
-    return (p >= 1.0) ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)(p * 0x1.0p64);
+__device__ __forceinline__ int kind_count(const Tile &s, int k) {
+    int n = 0;
+#pragma unroll
+    for (int w = 0; w < NWARP; w++) n += s.wcount[w][k];
+    return n;
 }
 
-__device__ void bin_setup(Tile &s, int j, double lam, double h) {
+// Per-realization state of a block for the passes whose realization index is data dependent,
+// indexed [slot][thread].
+struct Slots {
+    float acc[RPT][RB];
+    float comp[RPT][RB];
+};
+
+__device__ __forceinline__ int bin_kind(double lam) {
+    if (!(lam > 0.0)) return KIND_NONE;
+    if (lam < TINY) return KIND_TINY;
+    if (lam < PTRS_MIN) return KIND_SMALL;
+    if (lam <= TABLE_MAX) return KIND_TABLE;
+    if (lam < PTRS32_MAX) return KIND_PTRS32;
+    return KIND_WIDE;
+}
+
+__device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
     s.lam[j] = lam;
-    s.h[j] = h;
     s.hs[j] = (float)(h * (double)HSCALE);
-    int kind;
-    if (!(lam > 0.0)) kind = KIND_NONE;
-    else if (lam > NORMAL_THRESH) kind = KIND_NORMAL;
-    else if (lam < TINY) kind = KIND_TINY;
-    else if (lam < PTRS_MIN) kind = KIND_SMALL;
-    else if (lam < PTRS32_MAX) kind = KIND_PTRS32;
-    else kind = KIND_PTRS64;
-    s.kind[j] = kind;
     if (kind == KIND_TINY) {
-        s.t0[j] = sat64(exp(-lam));
-        s.tskip[j] = sat64(exp(-(double)RPT * lam));
+        // u < tskip <=> no source in RPT draws; 1 - e^(-RPT lambda) to FP32 relative precision
+        const float miss = -expm1f(-(float)RPT * (float)lam);
+        s.tskip[j] = ~__float2ull_rn(miss * 0x1.0p64f);
     } else if (kind == KIND_SMALL) {
-        double p = exp(-lam);
-        double cdf = p;
-        s.t0[j] = sat64(cdf);
-        int n = 1;
-        for (; n < NT && cdf < 1.0; n++) {
-            p = p * lam * c_inv[n];
-            cdf += p;
-            s.thr[n][j] = (unsigned int)(sat64(cdf) >> 32);
+        // P(n) in FP32 by the recursion P(n) = P(n-1) lambda / n, rounded to 32.32 fixed point and
+        // summed exactly; the last threshold is saturated (P(n >= 31) < 1e-8 for lambda < 10)
+        const float lf = (float)lam;
+        float p = expf(-lf);
+        unsigned long long cum = 0;
+        int n = 0;
+        for (; n < NT - 1; n++) {
+            if (n > 0) p = p * lf * c_invf[n];
+            cum += __float2uint_rn(p * 0x1.0p32f);
+            s.u.thr[n][j] = (cum < 0xFFFFFFFFull) ? (unsigned int)cum : 0xFFFFFFFFu;
+            if ((float)n > lf && p < 0x1.0p-34f) {
+                n++;
+                break;
+            }
         }
-        for (; n < NT; n++) s.thr[n][j] = 0xFFFFFFFFu;
-    } else if (kind == KIND_PTRS32) {
-        double slam = sqrt(lam);
-        double b = 0.931 + 2.53 * slam;
-        double a = -0.059 + 0.02483 * b;
-        double inva = 1.1239 + 1.1328 / (b - 3.4);
-        double vr = 0.9277 - 3.6224 / (b - 2.0);
-        double li = floor(lam);
-        s.b[j] = (float)b;
-        s.a[j] = (float)a;
-        s.vr[j] = (float)vr;
-        s.log_inva[j] = (float)log(inva);
+        for (; n < NT; n++) s.u.thr[n][j] = 0xFFFFFFFFu;
+    } else if (kind == KIND_TABLE || kind == KIND_PTRS32) {
+        const float lf = (float)lam;
+        const double li = floor(lam);
         s.lam_int[j] = (int)li;
-        s.frac43[j] = (float)((lam - li) + 0.43);
-        s.lamf[j] = (float)lam;
+        s.frac[j] = (float)(lam - li);
+        s.lamf[j] = lf;
+        if (kind == KIND_TABLE) {
+            const float sd = sqrtf(lf);
+            const int k_lo = max(0, (int)floorf(lf - TABLE_SIGMAS * sd - 2.0f));
+            const int S = min((int)ceilf(lf + TABLE_SIGMAS * sd + 6.0f) - k_lo + 1, TMAX);
+            s.tb_klo[j] = k_lo;
+            s.tb_S[j] = S;
+            s.tb_gb[j] = 32 - __clz(S - 1);   // ceil(log2 S), S >= 2
+        }
+        if (kind == KIND_PTRS32) {
+            const float slam = sqrtf(lf);
+            const float b = 0.931f + 2.53f * slam;
+            const float a = -0.059f + 0.02483f * b;
+            const float inva = 1.1239f + 1.1328f / (b - 3.4f);
+            const float vr = 0.9277f - 3.6224f / (b - 2.0f);
+            s.b[j] = b;
+            s.a[j] = a;
+            s.vr[j] = vr;
+            s.log_inva[j] = logf(inva);
+            s.loglam[j] = logf(lf);
+        }
     }
 }
 
-// log P(k; lambda) for k >= 16 in FP32: -bd0(k, lambda) - log(2 pi k)/2 - stirlerr(k)
-// (Loader 2000, "Fast and accurate computation of binomial probabilities").
-__device__ __forceinline__ float log_pmf32(int k, float d, float lamf) {
-    float kf = (float)k;
-    float bd0;
-    float sum = kf + lamf;
-    if (fabsf(d) < 0.1f * sum) {
-        float v = d / sum;
-        float s = d * v;
-        float ej = 2.0f * kf * v;
-        float v2 = v * v;
-#pragma unroll 1
-        for (int j = 1; j < 24; j++) {
-            ej *= v2;
-            float s1 = s + ej / (float)(2 * j + 1);
-            if (s1 == s) break;
-            s = s1;
-        }
-        bd0 = s;
-    } else {
-        bd0 = kf * logf(kf / lamf) + lamf - kf;
+// bd0(k, lambda) = k log(k / lambda) + lambda - k (Loader 2000) in FP32 from d = k - lambda, which
+// the caller forms exactly as (k - floor(lambda)) - frac(lambda).
+__device__ __forceinline__ float bd0_f32(float kk, float d, float lamf) {
+    const float v = d / (kk + lamf);
+    if (fabsf(v) < 0.1f) {
+        const float v2 = v * v;
+        return d * v + 2.0f * kk * v * v2 * (0.33333333f + v2 * (0.2f + v2 * (0.14285714f + v2 * 0.11111111f)));
     }
-    float ik2 = 1.0f / (kf * kf);
-    float stirl = (0.083333333333f - (0.0027777777778f - 0.00079365079365f * ik2) * ik2) / kf;
-    return -bd0 - 0.5f * logf(6.283185307179586f * kf) - stirl;
+    return kk * log1pf(d / lamf) - d;
+}
+
+__device__ __forceinline__ float stirlerr_f32(int k) {
+    if (k < 16) return c_stirl[k];
+    const float kk = (float)k;
+    const float ik2 = 1.0f / (kk * kk);
+    return (0.083333333333f - (0.0027777777778f - 0.00079365079365f * ik2) * ik2) / kk;
+}
+
+// P(k; lambda) in FP32, relative error ~1e-7 across the table range:
+// exp(-bd0 - stirlerr(k)) / sqrt(2 pi k), and exp(-lambda) at k = 0.
+__device__ __forceinline__ float pmf_f32(int k, int lam_int, float frac, float lamf) {
+    if (k == 0) return expf(-lamf);
+    const float kk = (float)k;
+    const float d = (float)(k - lam_int) - frac;
+    return expf(-bd0_f32(kk, d, lamf) - stirlerr_f32(k)) * rsqrtf(6.283185307179586f * kk);
 }
 
 // One PTRS attempt from the uniforms (U word, V word); returns k >= 0 on acceptance, -1 otherwise.
+// __logf's absolute error (< 2^-21 near 1, 3 ulp elsewhere) is far below the FP32 resolution of
+// the log-densities compared.
 __device__ __forceinline__ int ptrs32_attempt(const Tile &s, int j, uint32_t wu, uint32_t wv) {
-    const float b = s.b[j], a = s.a[j], frac43 = s.frac43[j];
-    float U = u24(wu) - 0.5f;
-    float V = u24(wv);
-    float us = 0.5f - fabsf(U);
-    if (us < 0.013f && V > us) return -1;
-    float kf = floorf((2.0f * a * __frcp_rn(us) + b) * U + frac43);
-    if (!(kf > -1.0e7f && kf < 1.0e7f)) return -1;
-    int k = s.lam_int[j] + (int)kf;
+    const float b = s.b[j], a = s.a[j], frac = s.frac[j], lamf = s.lamf[j];
+    const float U = u24(wu) - 0.5f;
+    const float V = u24(wv);
+    const float us = 0.5f - fabsf(U);
+    const float kf = floorf((2.0f * a / us + b) * U + (frac + 0.43f));
+    const bool in_range = (kf > -1.0e7f) && (kf < 1.0e7f) && !(us < 0.013f && V > us);
+    const int k = in_range ? s.lam_int[j] + (int)kf : -1;
     if (k < 0) return -1;
     if (us >= 0.07f && V <= s.vr[j]) return k;
-    float lhs = logf(V) + s.log_inva[j] - logf(a / (us * us) + b);
+    const float lhs = __logf(V) + s.log_inva[j] - __logf(a / (us * us) + b);
     float rhs;
     if (k < 16) {
-        double lam = s.lam[j];
-        rhs = (float)(-lam + (double)k * log(lam) - c_lgam[k]);
+        rhs = -lamf + (float)k * s.loglam[j] - s.lgam[k];
     } else {
-        float d = (float)(k - s.lam_int[j]) - (frac43 - 0.43f);
-        rhs = log_pmf32(k, d, s.lamf[j]);
+        // log P(k; lambda) = -bd0(k, lambda) - log(2 pi k) / 2 - stirlerr(k)
+        const float kk = (float)k;
+        const float d = (float)(k - s.lam_int[j]) - frac;
+        rhs = -bd0_f32(kk, d, lamf) - 0.5f * __logf(6.283185307179586f * kk) - stirlerr_f32(k);
     }
     return (lhs <= rhs) ? k : -1;
 }
 
-// Further PTRS attempts of realization r after a rejected first attempt.
-__device__ int ptrs32_retry(const Tile &s, int j, uint32_t kb, uint32_t r, uint32_t f, uint32_t dom, uint2 key,
-                            int *d_status) {
-    for (int att = 1; att < MAX_ATTEMPTS; att++) {
-        uint4 w = philox(make_uint4(kb, r, f, dom | W_RETRY | (uint32_t)att), key);
-        int k = ptrs32_attempt(s, j, w.x, w.y);
-        if (k >= 0) return k;
-        k = ptrs32_attempt(s, j, w.z, w.w);
-        if (k >= 0) return k;
-    }
-    hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-    return (int)floor(s.lam[j] + 0.5);
-}
-
-// PTRS in FP64 for 2^22 <= lambda <= 1e10
-__device__ double ptrs64(uint4 ctr, uint2 key, double lam, int *d_status) {
+// PTRS in FP64 for 2^22 <= lambda <= 1e10 (and for prefix events with lambda >= 10);
+// attempt `att` uses counter ctr with .w = (ctr.w | att).
+__device__ double ptrs64(uint4 ctr, const PhiloxKey &key, double lam, int *d_status) {
     double slam = sqrt(lam), loglam = log(lam);
     double b = 0.931 + 2.53 * slam;
     double a = -0.059 + 0.02483 * b;
     double inva = 1.1239 + 1.1328 / (b - 3.4);
     double vr = 0.9277 - 3.6224 / (b - 2.0);
+    const uint32_t w0 = ctr.w;
     for (int att = 0; att < MAX_ATTEMPTS; att++) {
-        ctr.w = (ctr.w & 0xF0000000u) | (uint32_t)att;
+        ctr.w = w0 | (uint32_t)att;
         uint4 w = philox(ctr, key);
         double U = u53(w.x, w.y) - 0.5;
         double V = u53(w.z, w.w);
@@ -248,52 +328,71 @@ __device__ double ptrs64(uint4 ctr, uint2 key, double lam, int *d_status) {
     return floor(lam + 0.5);
 }
 
-// Count of a small-lambda bin from a 64-bit uniform (u >= t0 already known to mean n >= 1).
-__device__ __forceinline__ int small_count(const Tile &s, int j, unsigned long long u, int *d_status) {
-    int n = 1;
-    const uint32_t hi = (uint32_t)(u >> 32);
-    while (n < NT && hi >= s.thr[n][j]) n++;
-    if (n < NT) return n;
-    // beyond the table: continue the CDF in FP64
-    double lam = s.lam[j];
-    double uu = (double)(u >> 11) * 0x1.0p-53;
-    double p = exp(-lam);
-    double cdf = p;
-    int m = 0;
-    while (uu >= cdf && m < MAX_INVERSION) {
-        m++;
-        p *= lam / m;
-        cdf += p;
-    }
-    if (m >= MAX_INVERSION) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-    return m < NT ? NT : m;
-}
-
-// Zero-truncated Poisson count for a tiny-lambda hit, by inversion in FP64 from a 53-bit uniform.
-__device__ int truncated_count(double lam, double v, int *d_status) {
-    double e = exp(-lam);
-    double p = lam * e / (1.0 - e);   // P(n = 1 | n >= 1)
-    double cdf = p;
-    int n = 1;
-    while (v >= cdf && n < MAX_INVERSION) {
-        n++;
-        p *= lam / n;
-        cdf += p;
-    }
-    if (n >= MAX_INVERSION) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-    return n;
-}
-
-// Real-valued draw for the PTRS64 / Normal kinds.
-__device__ double draw_wide(const Tile &s, int j, int kind, uint4 ctr, uint2 key, int *d_status) {
-    double lam = s.lam[j];
-    if (kind == KIND_PTRS64) return ptrs64(ctr, key, lam, d_status);
-    // Normal branch (cyutils.pyx:1328-1330)
+// Normal(lambda, sqrt(lambda)) by Box-Muller (cyutils.pyx:1328-1330)
+__device__ double normal_draw(uint4 ctr, const PhiloxKey &key, double lam) {
     uint4 w = philox(ctr, key);
     double u1 = 1.0 - u53(w.x, w.y);   // (0, 1]
     double u2 = u53(w.z, w.w);
     double z = sqrt(-2.0 * log(u1)) * cos(2.0 * HGB_PI * u2);
     return lam + sqrt(lam) * z;
+}
+
+// Zero-truncated Poisson for lambda < 10, by inversion in FP64 from a 53-bit uniform.
+__device__ int truncated_count(double lam, double v, int *d_status) {
+    double p = lam / expm1(lam);      // P(n = 1 | n >= 1)
+    double cdf = p;
+    int n = 1;
+    while (v >= cdf) {   // stops where the rounded CDF stops growing (v within an ulp of 1)
+        if (n >= MAX_INVERSION) {
+            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+            break;
+        }
+        n++;
+        p *= lam / n;
+        const double next = cdf + p;
+        if (next == cdf) break;
+        cdf = next;
+    }
+    return n;
+}
+
+// Zero-truncated Poisson for lambda < TINY in FP32 (P(n >= 2) ~ lambda / 2).
+__device__ int truncated_count_f32(float lam, float v, int *d_status) {
+    float p = lam / expm1f(lam);      // P(n = 1 | n >= 1)
+    float cdf = p;
+    int n = 1;
+    while (v >= cdf) {   // stops where the rounded CDF stops growing (v within an ulp of 1)
+        if (n >= 64) {
+            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+            break;
+        }
+        n++;
+        p *= lam / (float)n;
+        const float next = cdf + p;
+        if (next == cdf) break;
+        cdf = next;
+    }
+    return n;
+}
+
+// Count of a small-lambda bin beyond its 32-entry table (P < 1e-8 for lambda < 10).
+__device__ int small_tail(double lam, uint32_t u, int *d_status) {
+    double uu = ((double)u + 0.5) * 0x1.0p-32;
+    double p = exp(-lam);
+    double cdf = p;
+    int m = 0;
+    while (uu >= cdf) {
+        if (m >= MAX_INVERSION) {
+            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+            break;
+        }
+        m++;
+        p *= lam / m;
+        const double next = cdf + p;
+        if (next == cdf) break;
+        cdf = next;
+    }
+    return m < NT ? NT : m;
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
@@ -303,7 +402,14 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
     sum = t;
 }
 
-// ---- gather into loudest-first (F, B) order
+__device__ __forceinline__ void add_bg(Slots &st, int sl, int t, float x) {
+    float acc = st.acc[sl][t], comp = st.comp[sl][t];
+    kahan_add(acc, comp, x);
+    st.acc[sl][t] = acc;
+    st.comp[sl][t] = comp;
+}
+
+// ---- 1. gather into loudest-first (F, B) order
 __global__ void k_gather_sorted(const double *__restrict__ number, const double *__restrict__ h2fdf,
                                 const int32_t *__restrict__ order, long nb, int nf, double *__restrict__ lam_s,
                                 double *__restrict__ h_s) {
@@ -316,230 +422,674 @@ __global__ void k_gather_sorted(const double *__restrict__ number, const double 
     h_s[(long)f * nb + k] = h2fdf[src];
 }
 
-struct LoudArgs {
-    long nb;          // bins
-    int nf, nr, nl;   // frequencies, realizations, loudest slots
-    int nchunk;       // chunk c holds tiles c, c + nchunk, c + 2 nchunk, ...
-    uint2 key;
-};
+// ---- 2. cumulative expectation along the sorted bins: C[0] = 0, C[k + 1] = C[k] + max(lambda_k, 0)
+// (NaN counts as 0; with h_mask, bins whose h2fdf is zero count as 0 -- the parameter path skips
+// them).  Each frequency's bins are cut into CUM_SEG segments: k_cum_sum totals the segments,
+// k_cum_write scans each segment from the sum of the segments before it.
+constexpr int CUM_THREADS = 1024;
+constexpr int CUM_PER_THREAD = 4;
+constexpr int CUM_SEG = 16;
 
-// Per-realization state of a block, indexed [slot][thread].
-struct RealState {
-    float acc[RPT][RB];
-    float comp[RPT][RB];
-    int nfill[RPT][RB];
-};
+__device__ __forceinline__ double cum_term(const double *lam, const double *mask, long k) {
+    double x = lam[k];
+    x = (x > 0.0) ? x : 0.0;
+    if (mask && mask[k] == 0.0) x = 0.0;
+    return x;
+}
 
-// Output rows of one chunk: loudest values (and their sorted positions when chunks are merged),
-// the number of filled slots and the background sum.
-struct LoudOut {
-    double *ss;     // [(c * nf + f) * nr + r][nl]
-    int *pos;       // same shape, or NULL when there is one chunk
-    double *bg;     // [(c * nf + f) * nr + r]
-    int *cnt;       // same, or NULL
-};
-
-template <bool LOUD>
-__device__ __forceinline__ void take(RealState &st, int i, int n, double h, float hs, int nl, int kpos, double *ss,
-                                     int *pos) {
-    const int t = threadIdx.x;
-    if (LOUD) {
-        int nfill = st.nfill[i][t];
-        while (nfill < nl && n > 0) {
-            ss[nfill] = h;
-            if (pos) pos[nfill] = kpos;
-            n--;
-            nfill++;
-        }
-        st.nfill[i][t] = nfill;
+__global__ void __launch_bounds__(256) k_cum_sum(long nb, const double *__restrict__ lam_s,
+                                                 const double *__restrict__ h_mask, double *__restrict__ seg_tot) {
+    __shared__ double red[256];
+    const int f = blockIdx.y, sg = blockIdx.x, t = threadIdx.x;
+    const long seg = (nb + CUM_SEG - 1) / CUM_SEG;
+    const long k0 = (long)sg * seg, k1 = min(k0 + seg, nb);
+    const double *lam = lam_s + (long)f * nb;
+    const double *mask = h_mask ? h_mask + (long)f * nb : nullptr;
+    double local = 0.0;
+    for (long k = k0 + t; k < k1; k += 256) local += cum_term(lam, mask, k);
+    red[t] = local;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) red[t] += red[t + o];
+        __syncthreads();
     }
-    if (n > 0) {
-        float acc = st.acc[i][t], comp = st.comp[i][t];
-        kahan_add(acc, comp, (float)n * hs);
-        st.acc[i][t] = acc;
-        st.comp[i][t] = comp;
+    if (t == 0) seg_tot[(long)f * CUM_SEG + sg] = red[0];
+}
+
+__global__ void __launch_bounds__(CUM_THREADS) k_cum_write(long nb, const double *__restrict__ lam_s,
+                                                           const double *__restrict__ h_mask,
+                                                           const double *__restrict__ seg_tot,
+                                                           double *__restrict__ cum) {
+    __shared__ double wsum[CUM_THREADS / 32];
+    __shared__ double carry_s;
+    const int f = blockIdx.y, sg = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const long seg = (nb + CUM_SEG - 1) / CUM_SEG;
+    const long k0 = (long)sg * seg, k1 = min(k0 + seg, nb);
+    const double *lam = lam_s + (long)f * nb;
+    const double *mask = h_mask ? h_mask + (long)f * nb : nullptr;
+    double *C = cum + (long)f * (nb + 1);
+    if (t == 0) {
+        double c = 0.0;
+        for (int j = 0; j < sg; j++) c += seg_tot[(long)f * CUM_SEG + j];
+        carry_s = c;
+        if (sg == 0) C[0] = 0.0;
+    }
+    __syncthreads();
+    const long span = (long)CUM_THREADS * CUM_PER_THREAD;
+    for (long base = k0; base < k1; base += span) {
+        double v[CUM_PER_THREAD];
+        double local = 0.0;
+        const long kk = base + (long)t * CUM_PER_THREAD;
+#pragma unroll
+        for (int e = 0; e < CUM_PER_THREAD; e++) {
+            const long k = kk + e;
+            const double x = (k < k1) ? cum_term(lam, mask, k) : 0.0;
+            v[e] = x;
+            local += x;
+        }
+        double incl = local;   // inclusive warp scan of the thread totals
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            double ws = wsum[lane];
+            double wi = ws;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                double y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            wsum[lane] = wi - ws;   // exclusive warp offsets
+        }
+        __syncthreads();
+        double run = carry_s + wsum[warp] + (incl - local);
+#pragma unroll
+        for (int e = 0; e < CUM_PER_THREAD; e++) {
+            const long k = kk + e;
+            run += v[e];
+            if (k < k1) C[k + 1] = run;
+        }
+        __syncthreads();
+        if (t == CUM_THREADS - 1) carry_s = run;
+        __syncthreads();
     }
 }
 
-// Real-valued counts (PTRS64 / Normal) follow cyutils.pyx:1333-1342 literally.
-template <bool LOUD>
-__device__ __forceinline__ void take_real(RealState &st, int i, double num, double h, float hs, int nl, int kpos,
-                                          double *ss, int *pos) {
-    const int t = threadIdx.x;
-    if (LOUD) {
-        if (num < 1.0) return;
-        int nfill = st.nfill[i][t];
-        while (nfill < nl && num > 0.0) {
-            ss[nfill] = h;
-            if (pos) pos[nfill] = kpos;
+// C for every frequency into cum ((F, B + 1)); seg_tot is (F, CUM_SEG) scratch
+int cumulate(long nb, int nf, const double *lam_s, const double *h_mask, double *seg_tot, double *cum,
+             cudaStream_t st) {
+    dim3 grid(CUM_SEG, (unsigned)nf);
+    k_cum_sum<<<grid, 256, 0, st>>>(nb, lam_s, h_mask, seg_tot);
+    int rc = hgb::check_launch();
+    if (rc) return rc;
+    k_cum_write<<<grid, CUM_THREADS, 0, st>>>(nb, lam_s, h_mask, seg_tot, cum);
+    return hgb::check_launch();
+}
+
+// ---- 3. the loudest slots, thread per (f, r)
+struct PrefixArgs {
+    long nb;
+    int nf, nr, nl;
+    PhiloxKey key;
+};
+
+// Source parameters of the params path (cyutils.pyx:1541-1770): bin centres of the three axes,
+// the four (B, F) grids of hgb_param_grids, and the loudest-first order to map positions to bins.
+struct ParArgs {
+    const int32_t *order;
+    const double *mt, *mr, *rz;          // (M-1), (Q-1), (Z-1)
+    const double *grid[4];               // redz_mid, dcom, sepa, angs, (B, F)
+    const int *scale_log2;               // [7]
+    int nq, nz;                          // bins along mrat, redz
+    double *sspar;                       // (4, F, R, L)
+    double *bgp_par;                     // (7, F, R): the prefix remainder's weighted sums
+    double *part_par;                    // (C, 7, F, R): the chunks' weighted sums
+};
+
+__device__ __forceinline__ double bin_param(const ParArgs &p, long b, int nf, int f, int k) {
+    if (k == 0) return p.mt[b / ((long)p.nq * p.nz)];
+    if (k == 1) return p.mr[(b / p.nz) % p.nq];
+    if (k == 2) return p.rz[b % p.nz];
+    return p.grid[k - 3][b * nf + f];
+}
+
+template <bool PARAMS>
+__global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict__ lam_s,
+                              const double *__restrict__ h_s, const double *__restrict__ cum,
+                              double *__restrict__ hc2ss, double *__restrict__ bgp, int *__restrict__ qpos,
+                              int *d_status) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)a.nf * a.nr) return;
+    const int f = (int)(idx / a.nr), r = (int)(idx % a.nr);
+    const long nb = a.nb;
+    const double *lam = lam_s + (long)f * nb;
+    const double *h = h_s + (long)f * nb;
+    const double *C = cum + (long)f * (nb + 1);
+    double *ss = hc2ss + idx * a.nl;
+    const double total = C[nb];
+    int nfill = 0;
+    double bg = 0.0;
+    double wbg[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    long i = 0;
+    const uint32_t max_events = (uint32_t)a.nl + MAX_PREFIX_EXTRA;
+    for (uint32_t e = 0; nfill < a.nl && i < nb; e++) {
+        if (e >= max_events) {
+            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+            break;
+        }
+        const uint4 ctr = make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX);
+        const uint4 w = philox(ctr, a.key);
+        const double target = C[i] - log1p(-u53(w.x, w.y));   // C[i] + Exp(1)
+        if (!(total > target)) {   // no further source in this realization
+            i = nb;
+            break;
+        }
+        long lo = i, hi = nb - 1;   // smallest j >= i with C[j + 1] > target (C[nb] > target)
+        while (lo < hi) {
+            const long mid = lo + ((hi - lo) >> 1);
+            if (C[mid + 1] > target) hi = mid;
+            else lo = mid + 1;
+        }
+        const long j = lo;
+        const double lj = lam[j];
+        double num;
+        if (lj > NORMAL_THRESH) {
+            num = normal_draw(make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX | 0x8000u), a.key, lj);
+        } else if (lj < PTRS_MIN) {
+            num = (double)truncated_count(lj, u53(w.z, w.w), d_status);
+        } else {
+            num = 0.0;
+            for (int rep = 0; rep < 64 && num < 1.0; rep++)
+                num = ptrs64(make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX | ((uint32_t)(rep + 1) << 8)), a.key,
+                             lj, d_status);
+            if (num < 1.0) {
+                hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+                num = 1.0;
+            }
+        }
+        i = j + 1;
+        if (num < 1.0) continue;   // cyutils.pyx:1331-1332
+        const double cur = h[j];
+        if (PARAMS && cur == 0.0) continue;   // cyutils.pyx:1710 (not reached: such bins are masked in C)
+        const long bin = PARAMS ? (long)pa.order[j] : 0;
+        while (nfill < a.nl && num > 0.0) {   // cyutils.pyx:1336-1340, 1711-1723
+            ss[nfill] = cur;
+            if (PARAMS) {
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    pa.sspar[(((long)k * a.nf + f) * a.nr + r) * a.nl + nfill] = bin_param(pa, bin, a.nf, f, k);
+            }
             num -= 1.0;
             nfill++;
         }
-        st.nfill[i][t] = nfill;
+        bg += num * cur;
+        if (PARAMS) {
+#pragma unroll
+            for (int k = 0; k < 7; k++) wbg[k] += num * cur * bin_param(pa, bin, a.nf, f, k);
+        }
     }
-    if (num != 0.0) {
-        float acc = st.acc[i][t], comp = st.comp[i][t];
-        kahan_add(acc, comp, (float)(num * (double)hs));
-        st.acc[i][t] = acc;
-        st.comp[i][t] = comp;
+    for (int l = nfill; l < a.nl; l++) {
+        ss[l] = 0.0;
+        if (PARAMS) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) pa.sspar[(((long)k * a.nf + f) * a.nr + r) * a.nl + l] = 0.0;
+        }
+    }
+    bgp[idx] = bg;
+    if (PARAMS) {
+#pragma unroll
+        for (int k = 0; k < 7; k++) pa.bgp_par[(long)k * a.nf * a.nr + idx] = wbg[k];
+    }
+    qpos[idx] = (int)i;
+}
+
+// ---- 4. bulk background
+struct BulkArgs {
+    long nb;
+    int nf, nr;
+    int nchunk;        // chunk c holds tiles c, c + nchunk, c + 2 nchunk, ...
+    uint32_t domain;
+    PhiloxKey key;
+};
+
+// Builds the inversion table of one table-kind bin (lambda in [10, TABLE_MAX]) with one warp:
+// P(k) for k = k_lo .. k_lo + S - 1 in FP32 (the Loader form at every fourth entry, the recursion
+// P(k) = P(k-1) lambda / k in between), rounded to 32.32 fixed point, summed exactly in integers
+// (warp scan) into cdf[m] = floor(CDF 2^32), and the guide cells 2^gb >= S: guide[i] = smallest m
+// with cdf[m] > i 2^(32 - gb).  The mass outside the range (< 1e-11) goes to the end entries.
+__device__ void build_table_warp(const Tile &s, int j, unsigned int *cdf, unsigned short *guide, int lane) {
+    const int S = s.tb_S[j], k_lo = s.tb_klo[j], shift = 32 - s.tb_gb[j];
+    const int E = (S + 31) >> 5;
+    const int m0 = min(lane * E, S), m1 = min(m0 + E, S);
+    const int lam_int = s.lam_int[j];
+    const float frac = s.frac[j], lamf = s.lamf[j];
+    unsigned long long local = 0;
+    float p = 0.0f;
+    for (int m = m0; m < m1; m++) {
+        const int k = k_lo + m;
+        if (((m - m0) & 3) == 0) p = pmf_f32(k, lam_int, frac, lamf);
+        else p = __fdividef(p * lamf, (float)k);   // 2 ulp per step, three steps per anchor
+        const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
+        cdf[m] = qm;
+        local += qm;
+    }
+    unsigned long long incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    unsigned long long run = incl - local;
+    const unsigned long long cell = 1ull << shift;
+    const unsigned int ncell = 1u << (32 - shift);
+    unsigned long long prev = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;   // cdf[m0 - 1]
+    for (int m = m0; m < m1; m++) {
+        run += cdf[m];
+        const unsigned long long cur = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
+        cdf[m] = (unsigned int)cur;
+        const unsigned int lo = (m == 0) ? 0u : (unsigned int)((prev + cell - 1) >> shift);
+        const unsigned int hi = (m == S - 1) ? ncell : (unsigned int)((cur + cell - 1) >> shift);
+        for (unsigned int i = lo; i < hi; i++) guide[i] = (unsigned short)m;
+        prev = cur;
+    }
+    __syncwarp();
+}
+
+// The same table built by the whole block (for large tables): entries spread over all threads, the
+// integer prefix sums by a block scan.  Starts and ends with a barrier-protected table.
+__device__ void build_table_block(Tile &s, int j, unsigned int *cdf, unsigned short *guide) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int S = s.tb_S[j], k_lo = s.tb_klo[j], shift = 32 - s.tb_gb[j];
+    const int E = (S + RB - 1) / RB;
+    const int m0 = min(t * E, S), m1 = min(m0 + E, S);
+    const int lam_int = s.lam_int[j];
+    const float frac = s.frac[j], lamf = s.lamf[j];
+    unsigned long long local = 0;
+    float p = 0.0f;
+    for (int m = m0; m < m1; m++) {
+        const int k = k_lo + m;
+        if (((m - m0) & 3) == 0) p = pmf_f32(k, lam_int, frac, lamf);
+        else p = __fdividef(p * lamf, (float)k);
+        const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
+        cdf[m] = qm;
+        local += qm;
+    }
+    unsigned long long incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s.scan[warp] = incl;
+    __syncthreads();
+    unsigned long long run = incl - local;
+    for (int w = 0; w < warp; w++) run += s.scan[w];
+    const unsigned long long cell = 1ull << shift;
+    const unsigned int ncell = 1u << (32 - shift);
+    unsigned long long prev = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
+    for (int m = m0; m < m1; m++) {
+        run += cdf[m];
+        const unsigned long long cur = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
+        cdf[m] = (unsigned int)cur;
+        const unsigned int lo = (m == 0) ? 0u : (unsigned int)((prev + cell - 1) >> shift);
+        const unsigned int hi = (m == S - 1) ? ncell : (unsigned int)((cur + cell - 1) >> shift);
+        for (unsigned int i = lo; i < hi; i++) guide[i] = (unsigned short)m;
+        prev = cur;
+    }
+    __syncthreads();
+}
+
+// arena words of a table-kind bin: S cdf entries and 2^gb u16 guide cells
+__device__ __forceinline__ int table_words(const Tile &s, int j) { return s.tb_S[j] + (1 << (s.tb_gb[j] - 1)); }
+
+// SORTED: lam / h are the gathered (F, B) arrays and qpos gives each realization's first bulk
+// position; otherwise lam / h are the (B, F) grids and every bin belongs to the bulk.
+// Parameter path: the seven weighted background sums per realization, FP32 Kahan in dynamic
+// shared memory [k][slot][thread], each term n * h2fdf * 2^100 * p_k * 2^-e_k (e_k the frexp exponent
+// of max |p_k|, so every scaled parameter is at most 1).
+constexpr int NPAR = 7;
+constexpr size_t PAR_SMEM = sizeof(float) * (NPAR * RB + 2 * NPAR * RPT * RB);
+
+__device__ __forceinline__ void add_par(float *psm, int sl, int t, int j, float n) {
+    const float *pw = psm;
+    float *pacc = psm + NPAR * RB;
+    float *pcomp = pacc + NPAR * RPT * RB;
+#pragma unroll
+    for (int k = 0; k < NPAR; k++) {
+        const int o = (k * RPT + sl) * RB + t;
+        float acc = pacc[o], comp = pcomp[o];
+        kahan_add(acc, comp, n * pw[k * RB + j]);
+        pacc[o] = acc;
+        pcomp[o] = comp;
     }
 }
 
-// The realization kernel.  LOUD: loudest split over sorted bins (lam / h are the gathered (F, B)
-// arrays); otherwise the second-pass GWB over bins in grid order (lam / h are the (B, F) grids).
-// grid (chunk, frequency, realization group), RB threads.
-template <bool LOUD>
-__global__ void __launch_bounds__(RB, 6) k_realize(LoudArgs a, const double *__restrict__ lam_in,
-                                                const double *__restrict__ h_in, LoudOut out, int *d_status) {
+template <bool SORTED, bool PARAMS>
+__global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
+                                                          const double *__restrict__ h_in,
+                                                          const int *__restrict__ qpos, double *__restrict__ part,
+                                                          int *d_status) {
     __shared__ Tile s;
-    __shared__ RealState st;
+    __shared__ Slots st;
+    extern __shared__ float psm[];   // PARAMS only: PAR_SMEM bytes
+    __shared__ int q_min_s, q_max_s;
     const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
     const int r0 = blockIdx.z * RB * RPT + t;
-    const uint32_t dom = LOUD ? 0u : DOMAIN_GWB;
     int rpt = 0;   // realizations of this thread: r0 + i * RB, i < rpt
     while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
-    const long row0 = ((long)c * a.nf + f) * a.nr + r0;   // output row of slot 0; slot i adds i * RB
+    // register accumulators for the passes with a fixed realization slot
+    float acc_r[RPT], comp_r[RPT];
+    int qmin = 0x7FFFFFFF, qmax = 0;
+#pragma unroll
     for (int i = 0; i < RPT; i++) {
+        acc_r[i] = 0.0f;
+        comp_r[i] = 0.0f;
         st.acc[i][t] = 0.0f;
         st.comp[i][t] = 0.0f;
-        st.nfill[i][t] = 0;
+        int q = 0x7FFFFFFF;
+        if (i < rpt) q = SORTED ? qpos[(long)f * a.nr + r0 + i * RB] : 0;
+        if (i < rpt) {
+            qmin = min(qmin, q);
+            qmax = max(qmax, q);
+        }
     }
+    if (PARAMS) {
+        for (int o = t; o < 2 * NPAR * RPT * RB; o += RB) psm[NPAR * RB + o] = 0.0f;
+    }
+    if (t < 16) s.lgam[t] = c_lgam[t];
+    if (t == 0) {
+        q_min_s = 0x7FFFFFFF;
+        q_max_s = 0;
+    }
+    __syncthreads();
+    if (SORTED) {
+        atomicMin(&q_min_s, qmin);
+        atomicMax(&q_max_s, qmax);
+    }
+    __syncthreads();
+    const int block_qmin = SORTED ? q_min_s : 0;
+    const int block_qmax = SORTED ? q_max_s : 0;
+    const uint4 ctr0 = make_uint4(0u, (uint32_t)r0, (uint32_t)f, a.domain);
+    // first bulk position of slot sl, for the passes whose slot is data dependent
+    const int *q_row = SORTED ? qpos + (long)f * a.nr + r0 : nullptr;
     const long ntiles = (a.nb + RB - 1) / RB;
     for (long tile = c; tile < ntiles; tile += a.nchunk) {
         const long base = tile * RB;
         const int nt = (int)((a.nb - base) < RB ? (a.nb - base) : RB);
+        if (base + nt <= (long)block_qmin) continue;   // every bin precedes every realization's bulk
+        const bool check = SORTED && base < (long)block_qmax;
         __syncthreads();
+        int kind = KIND_NONE;
         if (t < nt) {
             const long b = base + t;
-            if (LOUD) bin_setup(s, t, lam_in[(long)f * a.nb + b], h_in[(long)f * a.nb + b]);
-            else bin_setup(s, t, lam_in[b * a.nf + f], h_in[b * a.nf + f]);
+            const double lam = SORTED ? lam_in[(long)f * a.nb + b] : lam_in[b * a.nf + f];
+            kind = bin_kind(lam);
+            if (kind != KIND_NONE) {
+                const double h = SORTED ? h_in[(long)f * a.nb + b] : h_in[b * a.nf + f];
+                if (PARAMS && h == 0.0) {
+                    kind = KIND_NONE;   // cyutils.pyx:1710: skipped
+                } else {
+                    bin_setup(s, t, kind, lam, h);
+                    s.pos[t] = (int)b;
+                    if (PARAMS) {
+                        const long bin = SORTED ? (long)pa.order[b] : b;
+#pragma unroll
+                        for (int k = 0; k < NPAR; k++)
+                            psm[k * RB + t] =
+                                (float)ldexp(h * (double)HSCALE * bin_param(pa, bin, a.nf, f, k), -pa.scale_log2[k]);
+                    }
+                }
+            }
+        }
+        // per-kind lists in bin order: warp ballots, then the warps' offsets
+        unsigned rank_mask = 0;
+#pragma unroll
+        for (int k = 1; k < NKIND; k++) {
+            const unsigned m = __ballot_sync(0xffffffffu, kind == k);
+            if (kind == k) rank_mask = m;
+            if (lane == 0) s.wcount[warp][k] = __popc(m);
         }
         __syncthreads();
-        if (rpt == 0) continue;
-        for (int j = 0; j < nt; j++) {
-            const int kind = s.kind[j];
-            if (kind == KIND_NONE) continue;
-            const uint32_t kb = (uint32_t)(base + j);
-            const int kpos = (int)(base + j);
-            const double h = s.h[j];
+        if (kind != KIND_NONE) {
+            int off = 0;
+            for (int w = 0; w < warp; w++) off += s.wcount[w][kind];
+            off += __popc(rank_mask & ((1u << lane) - 1u));
+            s.list[kind][off] = (unsigned char)t;
+        }
+        __syncthreads();
+
+        // ---- small lambda: per-bin 32-entry table, four realizations per Philox call
+        const int n_small = kind_count(s, KIND_SMALL);
+#pragma unroll 1
+        for (int li = 0; li < n_small; li++) {
+            const int j = s.list[KIND_SMALL][li];
+            const int pos = s.pos[j];
             const float hs = s.hs[j];
-            if (kind == KIND_TINY) {
-                // geometric skipping over the thread's realizations
-                uint4 w = philox(make_uint4(kb, (uint32_t)r0, (uint32_t)f, dom | W_SKIP), a.key);
-                unsigned long long u = w64(w.x, w.y);
-                if (rpt == RPT && u < s.tskip[j]) continue;
-                const double lam = s.lam[j];
-                int i = 0;
-                for (int step = 0; step < 2 * RPT + 2; step++) {
-                    if (step > 0) {
-                        w = philox(make_uint4(kb, (uint32_t)r0, (uint32_t)f, dom | W_SKIP | (uint32_t)step), a.key);
-                        u = w64(w.x, w.y);
+            const unsigned int t0 = s.u.thr[0][j];
+#pragma unroll
+            for (int call = 0; call < RPT / 4; call++) {
+                if (4 * call >= rpt) break;
+                uint4 ctr = ctr0;
+                ctr.x = (uint32_t)pos;
+                ctr.w |= W_SMALL | (uint32_t)call;
+                const uint4 w = philox(ctr, a.key);
+#pragma unroll
+                for (int m = 0; m < 4; m++) {
+                    const int sl = 4 * call + m;
+                    const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
+                    if (sl >= rpt || u < t0) continue;
+                    int n = 0;
+                    if (u >= s.u.thr[n + 15][j]) n += 16;
+                    if (u >= s.u.thr[n + 7][j]) n += 8;
+                    if (u >= s.u.thr[n + 3][j]) n += 4;
+                    if (u >= s.u.thr[n + 1][j]) n += 2;
+                    if (u >= s.u.thr[n][j]) n += 1;
+                    if (n == NT - 1 && u >= s.u.thr[NT - 1][j]) n = small_tail(s.lam[j], u, d_status);
+                    if (!check || pos >= __ldg(q_row + sl * RB)) {
+                        kahan_add(acc_r[sl], comp_r[sl], (float)n * hs);
+                        if (PARAMS) add_par(psm, sl, t, j, (float)n);
                     }
-                    double uu = ((double)(u >> 11) + 1.0) * 0x1.0p-53;   // (0, 1]
-                    double gap = floor(-log(uu) / lam);
-                    if (gap >= (double)(rpt - i)) break;
-                    i += (int)gap;
-                    int n = truncated_count(lam, u53(w.z, w.w), d_status);
-                    take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
-                               out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
-                    i++;
-                    if (i >= rpt) break;
                 }
-            } else if (kind == KIND_SMALL) {
-                const unsigned long long t0 = s.t0[j];
+            }
+        }
+
+        // ---- table kind: inversion tables of up to BATCH_MAX bins at a time, packed in the arena and
+        // built one per warp; four realizations per Philox call
+        const int n_table = kind_count(s, KIND_TABLE);
 #pragma unroll 1
-                for (int i = 0; i < rpt; i += 2) {
-                    uint4 w = philox(make_uint4(kb, (uint32_t)(r0 + i * RB), (uint32_t)f, dom | W_PAIR), a.key);
-                    unsigned long long u = w64(w.x, w.y);
-                    if (u >= t0) {
-                        int n = small_count(s, j, u, d_status);
-                        take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
-                                   out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
-                    }
-                    u = w64(w.z, w.w);
-                    if (i + 1 < rpt && u >= t0) {
-                        int n = small_count(s, j, u, d_status);
-                        take<LOUD>(st, i + 1, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)(i + 1) * RB) * a.nl,
-                                   out.pos ? out.pos + (row0 + (long)(i + 1) * RB) * a.nl : nullptr);
-                    }
-                }
-            } else if (kind == KIND_PTRS32) {
-#pragma unroll 1
-                for (int i = 0; i < rpt; i += 2) {
-                    const uint32_t ra = (uint32_t)(r0 + i * RB);
-                    uint4 w = philox(make_uint4(kb, ra, (uint32_t)f, dom | W_PAIR), a.key);
-                    int n = ptrs32_attempt(s, j, w.x, w.y);
-                    if (n < 0) n = ptrs32_retry(s, j, kb, ra, (uint32_t)f, dom, a.key, d_status);
-                    take<LOUD>(st, i, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
-                               out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
-                    if (i + 1 < rpt) {
-                        n = ptrs32_attempt(s, j, w.z, w.w);
-                        if (n < 0) n = ptrs32_retry(s, j, kb, ra + RB, (uint32_t)f, dom, a.key, d_status);
-                        take<LOUD>(st, i + 1, n, h, hs, a.nl, kpos, out.ss + (row0 + (long)(i + 1) * RB) * a.nl,
-                                   out.pos ? out.pos + (row0 + (long)(i + 1) * RB) * a.nl : nullptr);
-                    }
-                }
+        for (int li = 0; li < n_table;) {
+            // the batch (same on every thread): one large table, or up to BATCH_MAX small ones
+            const bool big = s.tb_S[s.list[KIND_TABLE][li]] > TABLE_WARP_MAX;
+            int K = 0, used = 0;
+            while (li + K < n_table && K < BATCH_MAX) {
+                const int jj = s.list[KIND_TABLE][li + K];
+                const int words = table_words(s, jj);
+                if (K > 0 && (big || s.tb_S[jj] > TABLE_WARP_MAX || used + words > ARENA_WORDS)) break;
+                used += words;
+                K++;
+            }
+            __syncthreads();   // the arena is free (previous batch, or the small-lambda pass)
+            if (big) {
+                const int j = s.list[KIND_TABLE][li];
+                build_table_block(s, j, s.u.arena, (unsigned short *)(s.u.arena + s.tb_S[j]));
             } else {
+                // each table to the least-loaded warp so far (by entries), lowest warp on ties
+                int load[NWARP] = {};
+                int off = 0;
+                for (int i = 0; i < K; i++) {
+                    const int j = s.list[KIND_TABLE][li + i];
+                    int wmin = 0;
+#pragma unroll
+                    for (int w = 1; w < NWARP; w++)
+                        if (load[w] < load[wmin]) wmin = w;
+                    load[wmin] += s.tb_S[j];
+                    if (wmin == warp)
+                        build_table_warp(s, j, s.u.arena + off, (unsigned short *)(s.u.arena + off + s.tb_S[j]),
+                                         lane);
+                    off += table_words(s, j);
+                }
+                __syncthreads();   // every table of the batch is ready
+            }
+            int off = 0;
 #pragma unroll 1
-                for (int i = 0; i < rpt; i++) {
-                    const uint32_t r = (uint32_t)(r0 + i * RB);
-                    double num = draw_wide(s, j, kind, make_uint4(kb, r, (uint32_t)f, dom | W_WIDE), a.key, d_status);
-                    take_real<LOUD>(st, i, num, h, hs, a.nl, kpos, out.ss + (row0 + (long)i * RB) * a.nl,
-                                    out.pos ? out.pos + (row0 + (long)i * RB) * a.nl : nullptr);
+            for (int i = 0; i < K; i++) {
+                const int j = s.list[KIND_TABLE][li + i];
+                const int pos = s.pos[j];
+                const float hs = s.hs[j];
+                const int k_lo = s.tb_klo[j], S = s.tb_S[j], shift = 32 - s.tb_gb[j];
+                const unsigned int *cdf = s.u.arena + off;
+                const unsigned short *guide = (const unsigned short *)(s.u.arena + off + S);
+                off += table_words(s, j);
+#pragma unroll
+                for (int call = 0; call < RPT / 4; call++) {
+                    if (4 * call >= rpt) break;
+                    uint4 ctr = ctr0;
+                    ctr.x = (uint32_t)pos;
+                    ctr.w |= W_TABLE | (uint32_t)call;
+                    const uint4 w = philox(ctr, a.key);
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const int sl = 4 * call + m;
+                        const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
+                        if (sl >= rpt) continue;
+                        int e = guide[u >> shift];
+                        while (e < S - 1 && u >= cdf[e]) e++;
+                        if (!check || pos >= __ldg(q_row + sl * RB)) {
+                            kahan_add(acc_r[sl], comp_r[sl], (float)(k_lo + e) * hs);
+                            if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + e));
+                        }
+                    }
+                }
+            }
+            li += K;
+        }
+
+        // ---- PTRS32: one loop per lane over its realizations, two attempts per Philox call
+        const int n_ptrs = kind_count(s, KIND_PTRS32);
+#pragma unroll 1
+        for (int li = 0; li < n_ptrs; li++) {
+            if (rpt == 0) break;
+            const int j = s.list[KIND_PTRS32][li];
+            const int pos = s.pos[j];
+            const float hs = s.hs[j];
+            uint4 ctr = ctr0;
+            ctr.x = (uint32_t)pos;
+            ctr.w |= W_PTRS;
+            int sl = 0, it = 0;
+            uint4 w = make_uint4(0, 0, 0, 0);
+#pragma unroll 1
+            while (sl < rpt) {
+                if ((it & 1) == 0) {
+                    uint4 cc = ctr;
+                    cc.w |= (uint32_t)(it >> 1);
+                    w = philox(cc, a.key);
+                }
+                const int k = (it & 1) ? ptrs32_attempt(s, j, w.z, w.w) : ptrs32_attempt(s, j, w.x, w.y);
+                it++;
+                if (k >= 0) {
+                    if (!check || pos >= __ldg(q_row + sl * RB)) {
+                        add_bg(st, sl, t, (float)k * hs);
+                        if (PARAMS) add_par(psm, sl, t, j, (float)k);
+                    }
+                    sl++;
+                } else if (it >= MAX_PTRS_ITERS) {
+                    hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
+                    const float kfix = floorf(s.lamf[j] + 0.5f);
+                    for (; sl < rpt; sl++)
+                        if (!check || pos >= __ldg(q_row + sl * RB)) {
+                            add_bg(st, sl, t, kfix * hs);
+                            if (PARAMS) add_par(psm, sl, t, j, kfix);
+                        }
+                }
+            }
+        }
+
+        // ---- tiny lambda: geometric skipping over the lane's realizations
+        const int n_tiny = kind_count(s, KIND_TINY);
+#pragma unroll 1
+        for (int li = 0; li < n_tiny; li++) {
+            if (rpt == 0) break;
+            const int j = s.list[KIND_TINY][li];
+            const int pos = s.pos[j];
+            uint4 ctr = ctr0;
+            ctr.x = (uint32_t)pos;
+            ctr.w |= W_SKIP;
+            uint4 w = philox(ctr, a.key);
+            if (rpt == RPT && w64(w.x, w.y) < s.tskip[j]) continue;
+            const float lf = (float)s.lam[j];
+            const float hs = s.hs[j];
+            int i = 0;
+            for (int step = 0; step < 2 * RPT + 2; step++) {
+                if (step > 0) {
+                    uint4 cc = ctr;
+                    cc.w |= (uint32_t)step;
+                    w = philox(cc, a.key);
+                }
+                // U = (u + 1) 2^-64 in (0, 1]: -ln U = -log1p(-x) with x = (2^64 - 1 - u) 2^-64
+                const float x = fminf(__ull2float_rn(~w64(w.x, w.y)) * 0x1.0p-64f, 0.99999994f);
+                const float gap = floorf(-log1pf(-x) / lf);
+                if (gap >= (float)(rpt - i)) break;
+                i += (int)gap;
+                const int n = truncated_count_f32(lf, u24(w.z), d_status);
+                if (!check || pos >= __ldg(q_row + i * RB)) {
+                    add_bg(st, i, t, (float)n * hs);
+                    if (PARAMS) add_par(psm, i, t, j, (float)n);
+                }
+                i++;
+                if (i >= rpt) break;
+            }
+        }
+
+        // ---- PTRS64 / Normal (real-valued counts, cyutils.pyx:1327-1330 / :887-891)
+        const int n_wide = kind_count(s, KIND_WIDE);
+#pragma unroll 1
+        for (int li = 0; li < n_wide; li++) {
+            const int j = s.list[KIND_WIDE][li];
+            const int pos = s.pos[j];
+            const double lam = s.lam[j];
+            const float hs = s.hs[j];
+            for (int sl = 0; sl < rpt; sl++) {
+                uint4 ctr = ctr0;
+                ctr.x = (uint32_t)pos;
+                ctr.w |= W_WIDE | ((uint32_t)sl << 8);
+                const double num = (lam > NORMAL_THRESH) ? normal_draw(ctr, a.key, lam) : ptrs64(ctr, a.key, lam, d_status);
+                if (!check || pos >= __ldg(q_row + sl * RB)) {
+                    add_bg(st, sl, t, (float)(num * (double)hs));
+                    if (PARAMS) add_par(psm, sl, t, j, (float)num);
                 }
             }
         }
     }
-    for (int i = 0; i < rpt; i++) {
-        const long row = row0 + (long)i * RB;
-        if (LOUD) {
-            const int nfill = st.nfill[i][t];
-            double *ss = out.ss + row * a.nl;
-            for (int l = nfill; l < a.nl; l++) ss[l] = 0.0;
-            if (out.cnt) out.cnt[row] = nfill;
-        }
-        out.bg[row] = ((double)st.acc[i][t] - (double)st.comp[i][t]) * HSCALE_INV;
+#pragma unroll
+    for (int i = 0; i < RPT; i++)
+        if (i < rpt)
+            part[((long)c * a.nf + f) * a.nr + r0 + (long)i * RB] =
+                (((double)acc_r[i] - (double)comp_r[i]) + ((double)st.acc[i][t] - (double)st.comp[i][t])) * HSCALE_INV;
+    if (PARAMS) {
+        const float *pacc = psm + NPAR * RB;
+        const float *pcomp = pacc + NPAR * RPT * RB;
+        for (int k = 0; k < NPAR; k++)
+            for (int i = 0; i < rpt; i++) {
+                const int o = (k * RPT + i) * RB + t;
+                pa.part_par[(((long)c * NPAR + k) * a.nf + f) * a.nr + r0 + (long)i * RB] =
+                    ldexp(((double)pacc[o] - (double)pcomp[o]) * HSCALE_INV, pa.scale_log2[k]);
+            }
     }
 }
 
-// Merge per-chunk partials: the global loudest slots are the smallest sorted positions among the
-// chunks' own loudest lists (each list is in position order); every other listed source and every
-// chunk background goes to the background.
-__global__ void k_loudest_merge(LoudArgs a, LoudOut part, double *__restrict__ hc2ss, double *__restrict__ hc2bg) {
+// ---- 5. background = prefix remainder + chunk partials (fixed order)
+__global__ void k_bg_reduce(int nchunk, long nfr, const double *__restrict__ bgp, const double *__restrict__ part,
+                            double *__restrict__ out) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (long)a.nf * a.nr) return;
-    const long stride = (long)a.nf * a.nr;
-    double *out = hc2ss + idx * a.nl;
-    // heads[c]: next unread entry of chunk c's list (chunks <= 255, lists <= nl <= 255)
-    unsigned char heads[256];
-    for (int c = 0; c < a.nchunk; c++) heads[c] = 0;
-    for (int l = 0; l < a.nl; l++) {
-        int best = -1, bpos = 0x7FFFFFFF;
-        for (int c = 0; c < a.nchunk; c++) {
-            long row = (long)c * stride + idx;
-            if (heads[c] < part.cnt[row]) {
-                int p = part.pos[row * a.nl + heads[c]];
-                if (p < bpos) {
-                    bpos = p;
-                    best = c;
-                }
-            }
-        }
-        if (best < 0) {
-            out[l] = 0.0;
-            continue;
-        }
-        long row = (long)best * stride + idx;
-        out[l] = part.ss[row * a.nl + heads[best]];
-        heads[best]++;
-    }
-    double bg = 0.0;
-    for (int c = 0; c < a.nchunk; c++) {
-        long row = (long)c * stride + idx;
-        for (int e = heads[c]; e < part.cnt[row]; e++) bg += part.ss[row * a.nl + e];
-        bg += part.bg[row];
-    }
-    hc2bg[idx] = bg;
+    if (idx >= nfr) return;
+    double acc = bgp ? bgp[idx] : 0.0;
+    for (int c = 0; c < nchunk; c++) acc += part[(long)c * nfr + idx];
+    out[idx] = acc;
 }
 
 // Replay: thread per (frequency, realization), sequential over the sorted bins (cyutils.pyx:1312-1344).
@@ -569,12 +1119,56 @@ __global__ void k_loudest_replay(long nb, int nf, int nr, int nl, const double *
     hc2bg[idx] = sum;
 }
 
-__global__ void k_gwb_reduce(int nchunk, long nfr, const double *__restrict__ part, double *__restrict__ gwb) {
+// Replay with parameters: thread per (frequency, realization), the reference's loop and operation
+// order (cyutils.pyx:1686-1770), round-to-nearest multiply / add / divide.
+__global__ void k_loudest_par_replay(long nb, int nf, int nr, int nl, const double *__restrict__ h_s, ParArgs pa,
+                                     const double *__restrict__ replay, double *__restrict__ hc2ss,
+                                     double *__restrict__ hc2bg, double *__restrict__ bgpar) {
+    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)nf * nr) return;
+    int f = (int)(idx / nr), r = (int)(idx % nr);
+    const double *hf = h_s + (long)f * nb;
+    const double *cnt = replay + ((long)r * nf + f) * nb;
+    double *ss = hc2ss + idx * nl;
+    for (int l = 0; l < nl; l++) {
+        ss[l] = 0.0;
+        for (int k = 0; k < 4; k++) pa.sspar[(((long)k * nf + f) * nr + r) * nl + l] = 0.0;
+    }
+    int ll = 0;
+    double sum = 0.0;
+    double w[NPAR] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (long k = 0; k < nb; k++) {
+        double num = cnt[k];
+        const double cur = hf[k];
+        if (num < 1.0 || cur == 0.0) continue;
+        const long bin = pa.order[k];
+        while (ll < nl && num > 0.0) {
+            ss[ll] = cur;
+            for (int q = 0; q < 4; q++) pa.sspar[(((long)q * nf + f) * nr + r) * nl + ll] = bin_param(pa, bin, nf, f, q);
+            num = __dsub_rn(num, 1.0);
+            ll++;
+        }
+        const double nc = __dmul_rn(num, cur);
+        sum = __dadd_rn(sum, nc);
+        for (int q = 0; q < NPAR; q++) w[q] = __dadd_rn(w[q], __dmul_rn(nc, bin_param(pa, bin, nf, f, q)));
+    }
+    hc2bg[idx] = sum;
+    for (int q = 0; q < NPAR; q++) bgpar[(long)q * nf * nr + idx] = __ddiv_rn(w[q], sum);
+}
+
+// hc2bg and bgpar of the parameter path: prefix remainder + chunk partials, then the weighted means.
+__global__ void k_bg_reduce_par(int nchunk, long nfr, const double *__restrict__ bgp, const double *__restrict__ part,
+                                ParArgs pa, double *__restrict__ hc2bg, double *__restrict__ bgpar) {
     long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nfr) return;
-    double acc = 0.0;
-    for (int c = 0; c < nchunk; c++) acc += part[(long)c * nfr + idx];
-    gwb[idx] = acc;
+    double bg = bgp[idx];
+    for (int c = 0; c < nchunk; c++) bg += part[(long)c * nfr + idx];
+    hc2bg[idx] = bg;
+    for (int k = 0; k < NPAR; k++) {
+        double w = pa.bgp_par[(long)k * nfr + idx];
+        for (int c = 0; c < nchunk; c++) w += pa.part_par[((long)c * NPAR + k) * nfr + idx];
+        bgpar[(long)k * nfr + idx] = w / bg;
+    }
 }
 
 __global__ void k_gwb_replay(long nb, int nf, int nr, const double *__restrict__ hc2, const double *__restrict__ replay,
@@ -596,62 +1190,102 @@ int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
 int choose_nchunk(long nb, int nf, int nr) {
     long blocks = (long)n_rgroups(nr) * nf;
-    long target = 152L * 7 * 2;   // two waves of resident blocks on 152 SMs
+    long target = 152L * 5 * 2;   // two waves of resident blocks on 152 SMs
     long nchunk = hgb::ceil_div(target, blocks);
     long maxc = hgb::ceil_div(nb, 8L * RB);
     if (nchunk > maxc) nchunk = maxc;
     if (nchunk < 1) nchunk = 1;
-    if (nchunk > 255) nchunk = 255;
+    if (nchunk > 65535) nchunk = 65535;
     return (int)nchunk;
 }
 
 struct LoudLayout {
-    size_t off_lam, off_h, off_ss, off_pos, off_bg, off_cnt, total;
+    size_t off_lam, off_h, off_cum, off_seg, off_q, off_bgp, off_part, total;
     int nchunk;
 };
 
-LoudLayout loud_layout(long nb, int nf, int nr, int nl, int mode) {
+LoudLayout loud_layout(long nb, int nf, int nr, int mode) {
     LoudLayout L{};
-    L.nchunk = (mode == HGB_RNG_PHILOX) ? choose_nchunk(nb, nf, nr) : 1;
+    L.nchunk = choose_nchunk(nb, nf, nr);
+    const long nfr = (long)nf * nr;
     size_t o = 0;
     L.off_lam = o;
     o += align256(sizeof(double) * nb * nf);
     L.off_h = o;
     o += align256(sizeof(double) * nb * nf);
-    if (L.nchunk > 1) {
-        long n = (long)L.nchunk * nf * nr;
-        long m = n * (nl > 0 ? nl : 1);
-        L.off_ss = o;
-        o += align256(sizeof(double) * m);
-        L.off_pos = o;
-        o += align256(sizeof(int) * m);
-        L.off_bg = o;
-        o += align256(sizeof(double) * n);
-        L.off_cnt = o;
-        o += align256(sizeof(int) * n);
+    if (mode == HGB_RNG_PHILOX) {
+        L.off_cum = o;
+        o += align256(sizeof(double) * (nb + 1) * nf);
+        L.off_seg = o;
+        o += align256(sizeof(double) * CUM_SEG * nf);
+        L.off_q = o;
+        o += align256(sizeof(int) * nfr);
+        L.off_bgp = o;
+        o += align256(sizeof(double) * nfr);
+        L.off_part = o;
+        o += align256(sizeof(double) * (size_t)L.nchunk * nfr);
     }
     L.total = o;
     return L;
 }
 
-LoudArgs make_args(long nb, int nf, int nr, int nl, int nchunk, uint64_t seed) {
-    LoudArgs a;
+BulkArgs bulk_args(long nb, int nf, int nr, int nchunk, uint64_t seed, uint32_t domain) {
+    BulkArgs a;
     a.nb = nb;
     a.nf = nf;
     a.nr = nr;
-    a.nl = nl;
     a.nchunk = nchunk;
-    a.key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+    a.domain = domain;
+    a.key = make_key(seed);
     return a;
+}
+
+// Measurement hook: events recorded around the bulk kernel when enabled (per host thread).
+thread_local bool g_bulk_timing = false;
+thread_local cudaEvent_t g_bulk_ev[2] = {nullptr, nullptr};
+thread_local bool g_bulk_recorded = false;
+
+int bulk_event(int k, cudaStream_t st) {
+    if (!g_bulk_timing) return HGB_OK;
+    cudaError_t err = cudaEventRecord(g_bulk_ev[k], st);
+    if (err != cudaSuccess) {
+        hgb::set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    if (k == 1) g_bulk_recorded = true;
+    return HGB_OK;
 }
 
 }  // namespace
 
 extern "C" {
 
+int hgb_bulk_timing(int enable) {
+    if (enable && !g_bulk_ev[0]) {
+        for (int k = 0; k < 2; k++) {
+            cudaError_t err = cudaEventCreate(&g_bulk_ev[k]);
+            if (err != cudaSuccess) {
+                hgb::set_cuda_error(err);
+                return HGB_ERR_CUDA;
+            }
+        }
+    }
+    g_bulk_timing = enable != 0;
+    g_bulk_recorded = false;
+    return HGB_OK;
+}
+
+float hgb_bulk_last_ms(void) {
+    if (!g_bulk_recorded) return -1.0f;
+    float ms = -1.0f;
+    if (cudaEventElapsedTime(&ms, g_bulk_ev[0], g_bulk_ev[1]) != cudaSuccess) return -1.0f;
+    return ms;
+}
+
 size_t hgb_loudest_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode) {
+    (void)nloud;
     if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
-    return loud_layout(n_bins, n_freq, nreals, nloud, mode).total;
+    return loud_layout(n_bins, n_freq, nreals, mode).total;
 }
 
 int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n_bins, int n_freq, int nreals,
@@ -663,7 +1297,7 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
     HGB_CHECK_ARG(nloud <= 255);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || replay);
-    HGB_CHECK_ARG(n_bins < (1L << 31) && n_freq <= 65535 && nreals < (1 << 30));
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
     if (nreals == 0) return HGB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (n_bins == 0) {
@@ -671,34 +1305,132 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
         cudaMemsetAsync(hc2bg, 0, sizeof(double) * (size_t)n_freq * nreals, st);
         return hgb::check_launch();
     }
-    LoudLayout L = loud_layout(n_bins, n_freq, nreals, nloud, mode);
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
     if (!workspace || workspace_bytes < L.total) return HGB_ERR_WORKSPACE;
     char *w = (char *)workspace;
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
-    long n = n_bins * n_freq;
+    const long n = n_bins * n_freq;
+    const long nfr = (long)n_freq * nreals;
     k_gather_sorted<<<(unsigned)hgb::ceil_div(n, 256), 256, 0, st>>>(number, h2fdf, order, n_bins, n_freq, lam_s, h_s);
     int rc = hgb::check_launch();
     if (rc) return rc;
     if (mode == HGB_RNG_REPLAY) {
-        long nt = (long)n_freq * nreals;
-        k_loudest_replay<<<(unsigned)hgb::ceil_div(nt, 128), 128, 0, st>>>(n_bins, n_freq, nreals, nloud, h_s, replay,
+        k_loudest_replay<<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(n_bins, n_freq, nreals, nloud, h_s, replay,
                                                                              hc2ss, hc2bg);
         return hgb::check_launch();
     }
-    LoudArgs a = make_args(n_bins, n_freq, nreals, nloud, L.nchunk, seed);
+    double *cum = (double *)(w + L.off_cum);
+    int *q = (int *)(w + L.off_q);
+    double *bgp = (double *)(w + L.off_bgp);
+    double *part = (double *)(w + L.off_part);
+    if ((rc = cumulate(n_bins, n_freq, lam_s, nullptr, (double *)(w + L.off_seg), cum, st))) return rc;
+    PrefixArgs pa;
+    pa.nb = n_bins;
+    pa.nf = n_freq;
+    pa.nr = nreals;
+    pa.nl = nloud;
+    pa.key = make_key(seed);
+    k_loud_prefix<false><<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(pa, ParArgs{}, lam_s, h_s, cum, hc2ss, bgp,
+                                                                            q, d_status);
+    if ((rc = hgb::check_launch())) return rc;
+    BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
-    if (a.nchunk == 1) {
-        LoudOut o{hc2ss, nullptr, hc2bg, nullptr};
-        k_realize<true><<<grid, RB, 0, st>>>(a, lam_s, h_s, o, d_status);
+    if ((rc = bulk_event(0, st))) return rc;
+    k_bulk<true, false><<<grid, RB, 0, st>>>(a, ParArgs{}, lam_s, h_s, q, part, d_status);
+    if ((rc = hgb::check_launch())) return rc;
+    if ((rc = bulk_event(1, st))) return rc;
+    k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, bgp, part, hc2bg);
+    return hgb::check_launch();
+}
+
+size_t hgb_loudest_par_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode) {
+    (void)nloud;
+    if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
+    size_t o = L.total;
+    if (mode == HGB_RNG_PHILOX) {
+        const size_t nfr = (size_t)n_freq * nreals;
+        o += align256(sizeof(double) * NPAR * nfr);                    // prefix weighted sums
+        o += align256(sizeof(double) * NPAR * (size_t)L.nchunk * nfr);  // chunk weighted sums
+    }
+    return o;
+}
+
+int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf, int n_m, int n_q, int n_z,
+                                       int n_freq, int nreals, int nloud, const int32_t *order, int mode,
+                                       uint64_t seed, const double *replay, const double *mt_cent,
+                                       const double *mr_cent, const double *rz_cent, const double *redz_mid,
+                                       const double *dcom, const double *sepa, const double *angs,
+                                       const int *scale_log2, double *hc2ss, double *hc2bg, double *sspar,
+                                       double *bgpar, void *workspace, size_t workspace_bytes, int *d_status,
+                                       void *stream) {
+    HGB_CHECK_ARG(number && h2fdf && order && hc2bg && bgpar && n_m >= 1 && n_q >= 1 && n_z >= 1);
+    HGB_CHECK_ARG(n_freq >= 1 && nreals >= 0 && nloud >= 0 && nloud <= 255);
+    HGB_CHECK_ARG(nloud == 0 || (hc2ss && sspar));
+    HGB_CHECK_ARG(mt_cent && mr_cent && rz_cent && redz_mid && dcom && sepa && angs);
+    HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
+    HGB_CHECK_ARG(mode == HGB_RNG_REPLAY ? replay != nullptr : scale_log2 != nullptr);
+    const long n_bins = (long)n_m * n_q * n_z;
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
+    if (nreals == 0) return HGB_OK;
+    const size_t need = hgb_loudest_par_workspace_bytes(n_bins, n_freq, nreals, nloud, mode);
+    if (!workspace || workspace_bytes < need) return HGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
+    char *w = (char *)workspace;
+    double *lam_s = (double *)(w + L.off_lam);
+    double *h_s = (double *)(w + L.off_h);
+    const long n = n_bins * n_freq;
+    const long nfr = (long)n_freq * nreals;
+    ParArgs pa{};
+    pa.order = order;
+    pa.mt = mt_cent;
+    pa.mr = mr_cent;
+    pa.rz = rz_cent;
+    pa.grid[0] = redz_mid;
+    pa.grid[1] = dcom;
+    pa.grid[2] = sepa;
+    pa.grid[3] = angs;
+    pa.scale_log2 = scale_log2;
+    pa.nq = n_q;
+    pa.nz = n_z;
+    pa.sspar = sspar;
+    k_gather_sorted<<<(unsigned)hgb::ceil_div(n, 256), 256, 0, st>>>(number, h2fdf, order, n_bins, n_freq, lam_s, h_s);
+    int rc = hgb::check_launch();
+    if (rc) return rc;
+    if (mode == HGB_RNG_REPLAY) {
+        k_loudest_par_replay<<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(n_bins, n_freq, nreals, nloud, h_s, pa,
+                                                                                 replay, hc2ss, hc2bg, bgpar);
         return hgb::check_launch();
     }
-    LoudOut part{(double *)(w + L.off_ss), (int *)(w + L.off_pos), (double *)(w + L.off_bg), (int *)(w + L.off_cnt)};
-    k_realize<true><<<grid, RB, 0, st>>>(a, lam_s, h_s, part, d_status);
-    rc = hgb::check_launch();
-    if (rc) return rc;
-    long nt = (long)n_freq * nreals;
-    k_loudest_merge<<<(unsigned)hgb::ceil_div(nt, 128), 128, 0, st>>>(a, part, hc2ss, hc2bg);
+    double *cum = (double *)(w + L.off_cum);
+    int *q = (int *)(w + L.off_q);
+    double *bgp = (double *)(w + L.off_bgp);
+    double *part = (double *)(w + L.off_part);
+    pa.bgp_par = (double *)(w + L.total);
+    pa.part_par = (double *)(w + L.total + align256(sizeof(double) * NPAR * nfr));
+    if ((rc = cumulate(n_bins, n_freq, lam_s, h_s, (double *)(w + L.off_seg), cum, st))) return rc;
+    PrefixArgs pf;
+    pf.nb = n_bins;
+    pf.nf = n_freq;
+    pf.nr = nreals;
+    pf.nl = nloud;
+    pf.key = make_key(seed);
+    k_loud_prefix<true><<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(pf, pa, lam_s, h_s, cum, hc2ss, bgp, q,
+                                                                           d_status);
+    if ((rc = hgb::check_launch())) return rc;
+    BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u);
+    dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
+    cudaError_t err = cudaFuncSetAttribute(k_bulk<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)PAR_SMEM);
+    if (err != cudaSuccess) {
+        hgb::set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    k_bulk<true, true><<<grid, RB, PAR_SMEM, st>>>(a, pa, lam_s, h_s, q, part, d_status);
+    if ((rc = hgb::check_launch())) return rc;
+    k_bg_reduce_par<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, bgp, part, pa, hc2bg, bgpar);
     return hgb::check_launch();
 }
 
@@ -714,7 +1446,7 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     HGB_CHECK_ARG(number && hc2 && gwb && n_bins >= 0 && n_freq >= 1 && nreals >= 0);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || replay);
-    HGB_CHECK_ARG(n_bins < (1L << 31) && n_freq <= 65535 && nreals < (1 << 30));
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
     if (nreals == 0) return HGB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (n_bins == 0) {
@@ -728,14 +1460,13 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     }
     if (!workspace || workspace_bytes < hgb_sam_poisson_gwb_workspace_bytes(n_bins, n_freq, nreals))
         return HGB_ERR_WORKSPACE;
-    LoudArgs a = make_args(n_bins, n_freq, nreals, 0, choose_nchunk(n_bins, n_freq, nreals), seed);
+    BulkArgs a = bulk_args(n_bins, n_freq, nreals, choose_nchunk(n_bins, n_freq, nreals), seed, DOMAIN_GWB);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
-    LoudOut o{nullptr, nullptr, (double *)workspace, nullptr};
-    k_realize<false><<<grid, RB, 0, st>>>(a, number, hc2, o, d_status);
+    k_bulk<false, false><<<grid, RB, 0, st>>>(a, ParArgs{}, number, hc2, nullptr, (double *)workspace, d_status);
     int rc = hgb::check_launch();
     if (rc) return rc;
     long nfr = (long)n_freq * nreals;
-    k_gwb_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, (double *)workspace, gwb);
+    k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, nullptr, (double *)workspace, gwb);
     return hgb::check_launch();
 }
 

@@ -5,7 +5,8 @@
 //      sweeps in point order, each point's 2x2 normal system solved with its precomputed inverse,
 //      until the largest relative change of a sweep falls below `grad_tol`.  One block per slice;
 //      the points of one wavefront level update concurrently and read exactly the neighbour values a
-//      sequential sweep would read, so the iterates equal the sequential ones.
+//      sequential sweep would read, so the iterates equal the sequential ones.  k_gradients_lv keeps
+//      the slice in shared memory when it fits (grids up to ~9000 points).
 //   2. k_clough_tocher: the C1 piecewise-cubic Clough-Tocher interpolant (centroid split) at every
 //      node of the regular (log m1, log m2) grid; NaN outside the hull; NaN or negative values are
 //      replaced by the value of the nearest point.
@@ -75,6 +76,140 @@ __global__ void k_gradients(hgb_scatter_plan P, const double *__restrict__ dens,
         if (converged) break;
     }
     if (!converged && threadIdx.x == 0) hgb::flag(d_status, HGB_STATUS_GRADIENT_NOT_CONVERGED);
+}
+
+// The same solve with the slice's values and gradients in shared memory, indexed by level-order
+// position (a level's points are contiguous), for grids whose state fits on one SM.  One warp per
+// slice: a level's points (about 20 at 91x81) share the warp's lanes, because the SM's FP64 pipe
+// costs the same per warp instruction however many lanes are active.  The static neighbour data of
+// the next level (first LV_REG edges of each point, and its inverse normal matrix) is loaded into
+// registers while the current level computes, so a level waits only on shared memory.  Operations
+// and their order are those of k_gradients.
+constexpr int LV_REG = 6;   // interior points of the triangulated grid have 6 neighbours
+
+struct LvPre {
+    int e0, e1;
+    int idx[LV_REG];
+    double2 w01[LV_REG], w23[LV_REG];
+    double2 q01, q23;
+};
+
+__device__ __forceinline__ void lv_load(const hgb_scatter_plan &P, const int *eptr, int p, bool active, LvPre &x) {
+    x.e0 = active ? eptr[p] : 0;
+    x.e1 = active ? eptr[p + 1] : 0;
+#pragma unroll
+    for (int k = 0; k < LV_REG; k++) {
+        if (x.e0 + k < x.e1) {
+            const long e = x.e0 + k;
+            x.idx[k] = __ldg(P.lv_nbr + e);
+            x.w01[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * e));
+            x.w23[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * e + 2));
+        }
+    }
+    if (active) {
+        x.q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
+        x.q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
+    }
+}
+
+__global__ void __launch_bounds__(32, 1) k_gradients_lv(hgb_scatter_plan P, const double *__restrict__ dens,
+                                                        int nz, double *__restrict__ vals,
+                                                        double *__restrict__ grads, int *d_status) {
+    extern __shared__ double sm[];
+    const int z = blockIdx.x, t = threadIdx.x;
+    const int n = P.n_mtot * P.n_mrat;
+    double *f = sm;                                  // [n]
+    double *g = f + n;                               // [n][2]
+    int *eptr = (int *)(g + 2 * n);                  // [n + 1]
+    int *lptr = eptr + n + 1;                        // [n_levels + 1]
+    for (int p = t; p < n; p += 32) {
+        const int i = P.level_vtx[p];
+        const double v = dens[(long)i * nz + z];
+        f[p] = v;
+        vals[(long)z * n + i] = v;
+        g[2 * p] = 0.0;
+        g[2 * p + 1] = 0.0;
+        eptr[p] = P.lv_nbr_ptr[p];
+    }
+    if (t == 0) eptr[n] = P.lv_nbr_ptr[n];
+    for (int l = t; l <= P.n_levels; l += 32) lptr[l] = P.level_ptr[l];
+    __syncwarp();
+    const int nlev = P.n_levels;
+    const double tol_lo = P.grad_tol * (1.0 - 1e-12);   // below this multiple of the scale: surely < tol
+    bool converged = false;
+    LvPre nxt;
+    lv_load(P, eptr, lptr[0] + t, t < lptr[1] - lptr[0], nxt);
+    for (int it = 0; it < P.grad_maxiter; it++) {
+        bool over = false;   // some point changed by >= grad_tol (relative) in this sweep
+        for (int lev = 0; lev < nlev; lev++) {
+            const int p0 = lptr[lev], p1 = lptr[lev + 1];
+            const LvPre cur = nxt;
+            {   // the next level (the first level again after the last), loaded ahead
+                const int nl = (lev + 1 < nlev) ? lev + 1 : 0;
+                const int q0 = lptr[nl], q1 = lptr[nl + 1];
+                lv_load(P, eptr, q0 + t, t < q1 - q0, nxt);
+            }
+            for (int p = p0 + t; p < p1; p += 32) {
+                const bool pre = (p == p0 + t);   // the prefetched slot; wider levels load directly
+                const double fi = f[p];
+                double sx = 0.0, sy = 0.0;
+                const int e0 = pre ? cur.e0 : eptr[p], e1 = pre ? cur.e1 : eptr[p + 1];
+                int e = e0;
+                if (pre) {
+#pragma unroll
+                    for (int k = 0; k < LV_REG; k++) {
+                        if (e0 + k < e1) {
+                            const int j = cur.idx[k];
+                            const double c =
+                                6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * cur.w01[k].x + g[2 * j + 1] * cur.w01[k].y);
+                            sx += c * cur.w23[k].x;
+                            sy += c * cur.w23[k].y;
+                        }
+                    }
+                    e = e0 + LV_REG;
+                }
+                for (; e < e1; e++) {
+                    const int j = __ldg(P.lv_nbr + e);
+                    const double2 w01 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
+                    const double2 w23 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
+                    const double c = 6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * w01.x + g[2 * j + 1] * w01.y);
+                    sx += c * w23.x;
+                    sy += c * w23.y;
+                }
+                double2 q01, q23;
+                if (pre) {
+                    q01 = cur.q01;
+                    q23 = cur.q23;
+                } else {
+                    q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
+                    q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
+                }
+                const double nx = q01.x * sx + q01.y * sy;
+                const double ny = q23.x * sx + q23.y * sy;
+                // relative change, divided out only where the comparison with the tolerance is
+                // close (the decision is that of change / scale < tol)
+                const double change = fmax(fabs(nx - g[2 * p]), fabs(ny - g[2 * p + 1]));
+                const double scale = fmax(1.0, fmax(fabs(nx), fabs(ny)));
+                g[2 * p] = nx;
+                g[2 * p + 1] = ny;
+                if (change >= tol_lo * scale) over = over || (change / scale >= P.grad_tol);
+            }
+            __syncwarp();
+        }
+        converged = !__any_sync(0xffffffffu, over);
+        if (converged) break;
+    }
+    if (!converged && t == 0) hgb::flag(d_status, HGB_STATUS_GRADIENT_NOT_CONVERGED);
+    for (int p = t; p < n; p += 32) {
+        const int i = P.level_vtx[p];
+        grads[2L * z * n + 2 * i] = g[2 * p];
+        grads[2L * z * n + 2 * i + 1] = g[2 * p + 1];
+    }
+}
+
+size_t gradients_lv_smem(const hgb_scatter_plan &P) {
+    const size_t n = (size_t)P.n_mtot * P.n_mrat;
+    return sizeof(double) * 3 * n + sizeof(int) * (n + 1) + sizeof(int) * (P.n_levels + 1);
 }
 
 // ---- 2. Clough-Tocher value at barycentric (l0, l1, l2) of triangle r
@@ -200,7 +335,16 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     double *gridA = (double *)w;
     cudaStream_t st = (cudaStream_t)stream;
 
-    k_gradients<<<n_redz, 256, 0, st>>>(P, dens, n_redz, vals, grads, d_status);
+    const size_t lv_smem = gradients_lv_smem(P);
+    int dev = 0, smem_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 64 <= (size_t)smem_optin) {
+        cudaFuncSetAttribute(k_gradients_lv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_smem);
+        k_gradients_lv<<<n_redz, 32, lv_smem, st>>>(P, dens, n_redz, vals, grads, d_status);
+    } else {
+        k_gradients<<<n_redz, 256, 0, st>>>(P, dens, n_redz, vals, grads, d_status);
+    }
     int rc = hgb::check_launch();
     if (rc) return rc;
     dim3 gct((unsigned)hgb::ceil_div((long)NN, 256), (unsigned)n_redz);

@@ -424,6 +424,20 @@ int hgb_scatter_plan_build(const double *mtot, int n_mtot, const double *mrat, i
         for (int l = 0; l <= nlev; l++) plan->level_ptr[l] = count[l];
         std::vector<int> fill(count.begin(), count.end() - 1);
         for (int i = 0; i < n; i++) plan->level_vtx[fill[level[i]]++] = i;
+        // level-order copies: a level's points are contiguous, neighbours keep their order
+        std::vector<int> pos_of(n);
+        for (int p = 0; p < n; p++) pos_of[plan->level_vtx[p]] = p;
+        int e = 0;
+        for (int p = 0; p < n; p++) {
+            const int i = plan->level_vtx[p];
+            plan->lv_nbr_ptr[p] = e;
+            for (int q = plan->nbr_ptr[i]; q < plan->nbr_ptr[i + 1]; q++, e++) {
+                plan->lv_nbr[e] = pos_of[plan->nbr_idx[q]];
+                for (int c = 0; c < 4; c++) plan->lv_nbr_w[4 * e + c] = plan->nbr_w[4 * q + c];
+            }
+            for (int c = 0; c < 4; c++) plan->lv_qinv[4 * p + c] = plan->vtx_qinv[4 * i + c];
+        }
+        plan->lv_nbr_ptr[n] = e;
     }
 
     // ---- regular (log m1, log m2) grid (sam.py:1349-1357)

@@ -113,9 +113,88 @@ __global__ void k_cells(BinGeom g, StrainArgs s, const double *__restrict__ mtot
     }
 }
 
+// single_sources.py:117-143 on one (bin, frequency): the redshift midpoints (same order as
+// cell_strain), -1 where not positive; comoving distance (+inf there); Kepler separation at the
+// rest-frame orbital frequency; angular separation.  IEEE semantics give the reference's inf / NaN
+// for the -1 bins.  Also records the largest finite magnitude of each grid (as a frexp exponent)
+// over the bins with nonzero strain.
+__global__ void k_param_grids(BinGeom g, const double *__restrict__ mt_cent, const double *__restrict__ fobs_cent,
+                              const double *__restrict__ redz_final, double nwtg, StrainArgs s,
+                              const double *__restrict__ h2fdf, double *__restrict__ rz_mid,
+                              double *__restrict__ dcom, double *__restrict__ sepa, double *__restrict__ angs,
+                              int *scale_log2) {
+    const long nb = (long)(g.nm - 1) * (g.nq - 1) * (g.nz - 1);
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nb * g.nf) return;
+    const int f = (int)(idx % g.nf);
+    const long b = idx / g.nf;
+    const int z = (int)(b % (g.nz - 1));
+    const int q = (int)((b / (g.nz - 1)) % (g.nq - 1));
+    const int m = (int)(b / ((long)(g.nz - 1) * (g.nq - 1)));
+    double r[2][2][2];
+#pragma unroll
+    for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+        for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++) r[ii][jj][kk] = redz_final[vtx(g, m + ii, q + jj, z + kk, f)];
+    const double a00 = 0.5 * (r[1][0][0] + r[0][0][0]);
+    const double a01 = 0.5 * (r[1][0][1] + r[0][0][1]);
+    const double a10 = 0.5 * (r[1][1][0] + r[0][1][0]);
+    const double a11 = 0.5 * (r[1][1][1] + r[0][1][1]);
+    const double b0 = 0.5 * (a10 + a00);
+    const double b1 = 0.5 * (a11 + a01);
+    double zb = 0.5 * (b1 + b0);
+    double dc = INFINITY;
+    if (zb > 0.0) dc = hgb::comoving_distance(s.dc_val, s.dc_der, s.dc_n, zb);
+    else zb = -1.0;
+    const double frst = fobs_cent[f] * (1.0 + zb);
+    const double w = 2.0 * HGB_PI * frst;
+    const double sp = pow(nwtg * mt_cent[m] / (w * w), 1.0 / 3.0);
+    const double an = sp / (dc / (1.0 + zb));
+    rz_mid[idx] = zb;
+    dcom[idx] = dc;
+    sepa[idx] = sp;
+    angs[idx] = an;
+    if (scale_log2 && (!h2fdf || h2fdf[idx] != 0.0)) {
+        const double v[4] = {zb, dc, sp, an};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (isfinite(v[k]) && v[k] != 0.0) {
+                int e;
+                frexp(v[k], &e);
+                atomicMax(scale_log2 + k, e);
+            }
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+int hgb_param_grids(const double *mt_cent, int n_mtot, int n_mrat, int n_redz, const double *fobs_orb_cent,
+                    int n_freq, const double *redz_final, double nwtg, const hgb_cosmo *cosmo,
+                    const double *h2fdf, double *redz_mid, double *dcom, double *sepa, double *angs,
+                    int *scale_log2, void *stream) {
+    HGB_CHECK_ARG(mt_cent && fobs_orb_cent && redz_final && cosmo && redz_mid && dcom && sepa && angs);
+    HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
+    HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
+    BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
+    StrainArgs s{0.0, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    cudaStream_t st = (cudaStream_t)stream;
+    if (scale_log2) {
+        cudaError_t err = cudaMemsetAsync(scale_log2, 0x80, 4 * sizeof(int), st);   // very negative
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+    }
+    const long n = (long)(n_mtot - 1) * (n_mrat - 1) * (n_redz - 1) * n_freq;
+    k_param_grids<<<(unsigned)hgb::ceil_div(n, 256), 256, 0, st>>>(g, mt_cent, fobs_orb_cent, redz_final, nwtg, s,
+                                                                   h2fdf, redz_mid, dcom, sepa, angs, scale_log2);
+    return hgb::check_launch();
+}
 
 int hgb_integrate_3dx1d(const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat, const double *redz,
                         int n_redz, const double *dln_freq, int n_freq, const double *dnum, double *number,

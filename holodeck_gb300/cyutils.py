@@ -1,7 +1,8 @@
 """GPU versions of the holodeck/cyutils.pyx functions on the SAM path.
 
-``loudest_hc_from_sorted`` (cyutils.pyx:1220-1264) and ``sam_poisson_gwb`` (cyutils.pyx:854-897)
-keep the reference's argument lists.  Two keyword arguments are added:
+``loudest_hc_from_sorted`` (cyutils.pyx:1220-1264), ``loudest_hc_and_par_from_sorted_redz``
+(cyutils.pyx:1541-1770) and ``sam_poisson_gwb`` (cyutils.pyx:854-897) keep the reference's argument
+lists.  Two keyword arguments are added:
 
 * ``seed``   -- 64-bit key of the Philox draws (default: fresh entropy, like the reference's
                unseeded ``PCG64()``);
@@ -98,6 +99,78 @@ def sam_poisson_gwb(dist, hc2, nreals, normal_threshold=1e10, seed=None, replay=
            N.ptr(ws), int(ws_bytes), st.ptr, N.stream_handle())
     _raise_status(st)
     return gwb if like_torch else D.to_host(gwb)
+
+
+def _frexp_exponent(values):
+    """frexp exponent of max |finite, nonzero value| (0 when there is none)."""
+    v = np.abs(np.asarray(values, dtype=np.float64))
+    v = v[np.isfinite(v) & (v > 0)]
+    return int(np.frexp(v.max())[1]) if v.size else 0
+
+
+def loudest_par_device(number, h2fdf, nreals, nloudest, order, mt, mr, rz, grids, grid_scales, seed=None,
+                       replay=None, status=None):
+    """Device (hc2ss, hc2bg, sspar, bgpar) of the parameter path (cyutils.pyx:1541-1770).
+
+    number / h2fdf / the four ``grids`` (redz_mid, dcom, sepa, angs) are device (M-1, Q-1, Z-1, F)
+    tensors, ``mt`` / ``mr`` / ``rz`` the bin centres (host arrays), ``order`` the int32 loudest-first
+    bin order and ``grid_scales`` a device int32[4] of the grids' frexp exponents (hgb_param_grids).
+    """
+    t = D.torch()
+    shape = tuple(number.shape)
+    nf = int(shape[-1])
+    nb = int(number.numel() // nf)
+    dev = number.device
+    hc2ss = t.empty((nf, nreals, nloudest), dtype=t.float64, device=dev)
+    hc2bg = t.empty((nf, nreals), dtype=t.float64, device=dev)
+    sspar = t.empty((4, nf, nreals, nloudest), dtype=t.float64, device=dev)
+    bgpar = t.empty((7, nf, nreals), dtype=t.float64, device=dev)
+    mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
+    rep = None
+    if replay is not None:
+        rep = D.as_device(replay)
+        if tuple(rep.shape) != (nreals, nf, nb):
+            raise ValueError(f"replay must be shaped (R, F, B)=({nreals}, {nf}, {nb}), got {tuple(rep.shape)}")
+    mt_d, mr_d, rz_d = (D.as_device(np.ascontiguousarray(x, dtype=np.float64), dev) for x in (mt, mr, rz))
+    scales = t.cat([t.tensor([_frexp_exponent(x) for x in (mt, mr, rz)], dtype=t.int32, device=dev),
+                    grid_scales.to(t.int32)])
+    lib = N.load()
+    ws_bytes = lib.hgb_loudest_par_workspace_bytes(nb, nf, int(nreals), int(nloudest), mode)
+    ws = D.workspace(ws_bytes, dev)
+    st = status if status is not None else D.StatusWord(dev)
+    seed = new_seed() if seed is None else int(seed) & 0xFFFFFFFFFFFFFFFF
+    N.call("hgb_loudest_hc_and_par_from_sorted", N.ptr(number), N.ptr(h2fdf), int(shape[0]), int(shape[1]),
+           int(shape[2]), nf, int(nreals), int(nloudest), N.ptr(order), mode, seed, N.ptr(rep), N.ptr(mt_d),
+           N.ptr(mr_d), N.ptr(rz_d), *[N.ptr(g) for g in grids], N.ptr(scales), N.ptr(hc2ss), N.ptr(hc2bg),
+           N.ptr(sspar), N.ptr(bgpar), N.ptr(ws), int(ws_bytes), st.ptr, N.stream_handle())
+    return hc2ss, hc2bg, sspar, bgpar
+
+
+def loudest_hc_and_par_from_sorted_redz(number, h2fdf, nreals, nloudest, mt, mr, rz, redz_final, dcom_final, sepa,
+                                        angs, msort, qsort, zsort, normal_threshold=1e10, seed=None, replay=None):
+    """(hc2ss (F, R, L), hc2bg (F, R), sspar (4, F, R, L), bgpar (7, F, R)); cyutils.pyx:1541-1770.
+
+    Same arguments as the reference (the (M, Q, Z, F) grids as numpy arrays or device tensors);
+    ``seed`` / ``replay`` as in :func:`loudest_hc_from_sorted`.
+    """
+    _check_threshold(normal_threshold)
+    like_torch = D.is_torch(number)
+    shape = tuple(number.shape)
+    num = D.as_device(number)
+    hh = D.as_device(h2fdf)
+    grids = [D.as_device(np.broadcast_to(np.asarray(D.to_host(g) if D.is_torch(g) else g), shape).copy()
+                         if not D.is_torch(g) else g).contiguous() for g in (redz_final, dcom_final, sepa, angs)]
+    t = D.torch()
+    scales = t.tensor([_frexp_exponent(D.to_host(g)[D.to_host(hh) != 0]) for g in grids], dtype=t.int32,
+                      device=num.device)
+    ms, qs, zs = [np.asarray(D.to_host(v) if D.is_torch(v) else v, dtype=np.int64) for v in (msort, qsort, zsort)]
+    order = D.as_device(np.ravel_multi_index((ms, qs, zs), shape[:3]), dtype=t.int32)
+    st = D.StatusWord()
+    out = loudest_par_device(num, hh, int(nreals), int(nloudest), order, D.to_host(mt) if D.is_torch(mt) else mt,
+                             D.to_host(mr) if D.is_torch(mr) else mr, D.to_host(rz) if D.is_torch(rz) else rz,
+                             grids, scales, seed=seed, replay=replay, status=st)
+    _raise_status(st)
+    return out if like_torch else tuple(D.to_host(x) for x in out)
 
 
 def _raise_status(st):

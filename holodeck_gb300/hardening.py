@@ -20,6 +20,17 @@ class Hard_GW(_Hardening):
         return False
 
 
+_SIDE_STREAMS = {}
+
+
+def _side_stream(dev):
+    t = D.torch()
+    key = str(dev)
+    if key not in _SIDE_STREAMS:
+        _SIDE_STREAMS[key] = t.cuda.Stream(device=dev)
+    return _SIDE_STREAMS[key]
+
+
 class Fixed_Time_2PL_SAM(_Hardening):
     """Two-power-law hardening normalised to a fixed total lifetime (hardening.py:1371-1457).
 
@@ -38,10 +49,21 @@ class Fixed_Time_2PL_SAM(_Hardening):
         assert np.ndim(gamma_outer) == 0
         t = D.torch()
         mt_d, mr_d = sam._edges_device()[:2]
-        mtot, mrat = t.meshgrid(mt_d, mr_d, indexing="ij")
-        shape = tuple(mtot.shape)
-        nl, norm = sam_cyutils.find_2pwl_hardening_norm(time, mtot.reshape(-1), mrat.reshape(-1), sepa_init, rchar,
-                                                        gamma_inner, gamma_outer, num_steps, return_norm=True)
+        # The root finding depends only on the mass grid: it runs on a side stream, concurrently with the
+        # density and scatter stages that the next gwb() call enqueues, and the dbn stage waits on it.
+        main = t.cuda.current_stream(mt_d.device)
+        side = _side_stream(mt_d.device)
+        side.wait_stream(main)
+        with t.cuda.stream(side):
+            mtot, mrat = t.meshgrid(mt_d, mr_d, indexing="ij")
+            shape = tuple(mtot.shape)
+            nl, norm = sam_cyutils.find_2pwl_hardening_norm(time, mtot.reshape(-1), mrat.reshape(-1), sepa_init,
+                                                            rchar, gamma_inner, gamma_outer, num_steps,
+                                                            return_norm=True)
+            self._norm_ready = t.cuda.Event()
+            self._norm_ready.record(side)
+        for x in (nl, norm):
+            x.record_stream(main)   # freed memory is not reused before the main stream is done with it
         self._norm_t = norm.reshape(shape)
         self._norm_log10_t = nl.reshape(shape)
         self._norm_host = None
@@ -56,10 +78,12 @@ class Fixed_Time_2PL_SAM(_Hardening):
     def _norm(self):
         """Hardening-rate normalisation per (mtot, mrat) cell (numpy, like hardening.py:1416)."""
         if self._norm_host is None:
-            self._norm_host = D.to_host(self._norm_t)
+            self._norm_host = D.to_host(self._norm_device())
         return self._norm_host
 
     def _norm_device(self):
+        """The device normalisation, ordered before the work enqueued next on the current stream."""
+        D.torch().cuda.current_stream(self._norm_t.device).wait_event(self._norm_ready)
         return self._norm_t
 
     def __str__(self):

@@ -189,8 +189,9 @@ class Semi_Analytic_Model:
 
     # ---- GWB (sam.py:872-947)
 
-    def gwb_device(self, fobs_gw_edges, hard=None, realize=100, loudest=1, seed=None, replay=None, order=None):
-        """Device (hc_ss[F, R, L], hc_bg[F, R]) tensors; see :meth:`gwb`."""
+    def gwb_device(self, fobs_gw_edges, hard=None, realize=100, loudest=1, seed=None, replay=None, order=None,
+                   params=False):
+        """Device (hc_ss[F, R, L], hc_bg[F, R]) tensors, plus (sspar, bgpar) with ``params``; see :meth:`gwb`."""
         hard = hardening.Hard_GW() if hard is None else hard
         if not isinstance(hard, (hardening.Fixed_Time_2PL_SAM, hardening.Hard_GW)):
             raise ValueError("`sam_cyutils` methods only work with `Fixed_Time_2PL_SAM` or `Hard_GW` hardening "
@@ -203,6 +204,10 @@ class Semi_Analytic_Model:
         fobs_orb_cents = fobs_gw_cents / 2.0
         redz_final, diff_num = self._dbn_device(hard, fobs_orb_cents)
         number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final)
+        if params:
+            edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]
+            return single_sources.ss_params_device(edges, redz_final, number, h2fdf, realize, loudest, seed=seed,
+                                                   replay=replay, order=order, cosmo=self._cosmo)
         return single_sources.ss_realize_device(number, h2fdf, realize, loudest, seed=seed, replay=replay,
                                                 order=order)
 
@@ -226,16 +231,16 @@ class Semi_Analytic_Model:
 
     def gwb(self, fobs_gw_edges, hard=None, realize=100, loudest=1, params=False, seed=None, replay=None,
             order=None, return_torch=False):
-        """Characteristic strain of the L loudest sources (F, R, L) and of the background (F, R).
+        """Characteristic strain of the L loudest sources (F, R, L) and of the background (F, R), and
+        with ``params=True`` the loudest sources' (M, q, z, z_final) (4, F, R, L) and the background's
+        weighted-mean parameters (7, F, R).
 
         Same arguments and results as sam.py:872-947.  Added keywords: ``seed`` (Philox key; default
         fresh entropy), ``replay``/``order`` (replay an externally drawn Poisson stream bit for bit),
         ``return_torch`` (keep the results on the device).
         """
-        if params:
-            raise NotImplementedError("params=True (sspar/bgpar) is not on the GPU path yet")
-        hc_ss, hc_bg = self.gwb_device(fobs_gw_edges, hard=hard, realize=realize, loudest=loudest, seed=seed,
-                                       replay=replay, order=order)
+        out = self.gwb_device(fobs_gw_edges, hard=hard, realize=realize, loudest=loudest, seed=seed,
+                              replay=replay, order=order, params=params)
         if return_torch:
-            return hc_ss, hc_bg
-        return D.to_host(hc_ss), D.to_host(hc_bg)
+            return out
+        return tuple(D.to_host(x) for x in out)

@@ -22,7 +22,8 @@ GRAD_MAXITER = 400     # CloughTocher2DInterpolator default sweep limit
 _DTYPES = dict(pts=np.float64, tri=np.int32, tri_kappa=np.float64, vtx_qinv=np.float64, nbr_ptr=np.int32,
                nbr_idx=np.int32, nbr_w=np.float64, level_ptr=np.int32, level_vtx=np.int32, grid_tri=np.int32,
                grid_bary=np.float64, grid_near=np.int32, grid_axis=np.float64, weights=np.float64,
-               back_idx=np.int32, back_t=np.float64, back_w=np.float64)
+               back_idx=np.int32, back_t=np.float64, back_w=np.float64, lv_nbr_ptr=np.int32, lv_nbr=np.int32,
+               lv_nbr_w=np.float64, lv_qinv=np.float64)
 
 _PLANS = {}
 
@@ -39,7 +40,7 @@ def host_plan(mtot, mrat, scatter, refine=4):
                   nbr_idx=(nnbr,), nbr_w=(nnbr, 4), level_ptr=(nlev + 1,), level_vtx=(npts,),
                   grid_tri=(ngrid * ngrid,), grid_bary=(ngrid * ngrid, 3), grid_near=(ngrid * ngrid,),
                   grid_axis=(ngrid,), weights=(ngrid, ngrid), back_idx=(npts, 2), back_t=(npts, 2),
-                  back_w=(npts, ngrid))
+                  back_w=(npts, ngrid), lv_nbr_ptr=(npts + 1,), lv_nbr=(nnbr,), lv_nbr_w=(nnbr, 4), lv_qinv=(npts, 4))
     arrs = {kk: np.zeros(shapes[kk], dtype=_DTYPES[kk]) for kk in N._SCATTER_ARRAYS}
     hp = N.HgbScatterHostPlan(**{kk: arrs[kk].ctypes.data_as(ctypes.c_void_p) for kk in N._SCATTER_ARRAYS})
     sz = N.HgbScatterSizes()
@@ -50,6 +51,8 @@ def host_plan(mtot, mrat, scatter, refine=4):
     arrs["tri_kappa"] = arrs["tri_kappa"][:sz.n_tri]
     arrs["nbr_idx"] = arrs["nbr_idx"][:sz.n_nbr]
     arrs["nbr_w"] = arrs["nbr_w"][:sz.n_nbr]
+    arrs["lv_nbr"] = arrs["lv_nbr"][:sz.n_nbr]
+    arrs["lv_nbr_w"] = arrs["lv_nbr_w"][:sz.n_nbr]
     arrs["level_ptr"] = arrs["level_ptr"][:sz.n_levels + 1]
     return arrs, sz
 

@@ -141,6 +141,11 @@ typedef struct {    /* host arrays, sized by hgb_scatter_plan_bounds */
     int32_t *back_idx;  /* [n_pts][2] lower grid cell */
     double *back_t;     /* [n_pts][2] fractional offsets */
     double *back_w;     /* [n_pts][n_grid] (1-tx) (W W)[:, a] + tx (W W)[:, a+1] */
+    /* the neighbourhoods again, indexed by level-order position p (point level_vtx[p]) */
+    int32_t *lv_nbr_ptr; /* [n_pts+1] */
+    int32_t *lv_nbr;    /* [n_nbr] neighbour positions, in the order of nbr_idx */
+    double *lv_nbr_w;   /* [n_nbr][4] */
+    double *lv_qinv;    /* [n_pts][4] */
 } hgb_scatter_host_plan;
 
 typedef struct {    /* the same arrays on the device */
@@ -161,6 +166,10 @@ typedef struct {    /* the same arrays on the device */
     const int32_t *back_idx;
     const double *back_t;
     const double *back_w;
+    const int32_t *lv_nbr_ptr;
+    const int32_t *lv_nbr;
+    const double *lv_nbr_w;
+    const double *lv_qinv;
     double grad_tol;    /* 1e-6 in the reference */
     int grad_maxiter;   /* 400 in the reference */
 } hgb_scatter_plan;
@@ -256,6 +265,58 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
                                int nreals, int nloud, const int32_t *order, int mode, uint64_t seed,
                                const double *replay, double *hc2ss, double *hc2bg,
                                void *workspace, size_t workspace_bytes, int *d_status, void *stream);
+
+/* Parameter grids of ss_gws_redz(params=True) (single_sources.py:117-143) on the (B, F) bins:
+ * redz_mid = the redshift midpoints of redz_final along mtot, mrat, redz (-1 where <= 0),
+ * dcom = comoving distance of redz_mid (+inf where it is -1), sepa = Kepler separation
+ * (G mt / (2 pi fobs_orb_cent (1 + redz_mid))^2)^(1/3) with mt the bin-centre total mass, and
+ * angs = sepa / (dcom / (1 + redz_mid)).  mt_cent (M-1) and fobs_orb_cent (F) are device arrays of
+ * the axis midpoints; nwtg is the gravitational constant of holodeck.constants (astropy's).
+ * scale_log2 (device int[4], may be NULL) receives, per output grid, the exponent e of
+ * max |finite value| (frexp convention, over bins with a nonzero h2fdf when h2fdf is given). */
+int hgb_param_grids(const double *mt_cent, int n_mtot, int n_mrat, int n_redz, const double *fobs_orb_cent,
+                    int n_freq, const double *redz_final, double nwtg, const hgb_cosmo *cosmo,
+                    const double *h2fdf, double *redz_mid, double *dcom, double *sepa, double *angs,
+                    int *scale_log2, void *stream);
+
+/* Loudest-L split with source parameters.  Replaces cyutils.loudest_hc_and_par_from_sorted_redz,
+ * cyutils.pyx:1541-1770: as hgb_loudest_hc_from_sorted, but bins with h2fdf == 0 are skipped
+ * (neither slots nor background), each filled slot also records
+ * sspar[0..3, f, r, l] = (mt_cent[m], mr_cent[q], rz_cent[z], redz_mid[b, f]) of its bin
+ * b = (m, q, z), and bgpar[k, f, r] = sum(n h2fdf p_k) / sum(n h2fdf) over the background
+ * sources for the seven parameters p = (mt, mr, rz, redz_mid, dcom, sepa, angs) (0/0 = NaN as in
+ * the reference).  The grids are the outputs of hgb_param_grids; scale_log2 (device int[7]: the
+ * frexp exponents of max |p_k| for mt, mr, rz and the four grids) sets the FP32 scaling of the
+ * Philox-mode background sums.  sspar is (4, F, R, L), bgpar (7, F, R).  Replay mode reproduces
+ * the reference bit for bit. */
+size_t hgb_loudest_par_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode);
+int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf, int n_m, int n_q, int n_z,
+                                       int n_freq, int nreals, int nloud, const int32_t *order, int mode,
+                                       uint64_t seed, const double *replay, const double *mt_cent,
+                                       const double *mr_cent, const double *rz_cent, const double *redz_mid,
+                                       const double *dcom, const double *sepa, const double *angs,
+                                       const int *scale_log2, double *hc2ss, double *hc2bg, double *sspar,
+                                       double *bgpar, void *workspace, size_t workspace_bytes, int *d_status,
+                                       void *stream);
+
+/* Model details of a library run.  Replaces librarian/lib_tools.py:845-943 (_calc_model_details):
+ * with w = h2fdf * number on the (M-1, Q-1, Z-1, F) bins, gwb_m (M-1, Z-1, F), gwb_q (Q-1, Z-1, F)
+ * and gwb_z (Z-1, F) are the sums of w over the other mass axes divided by denom[f] = sum(w);
+ * gwb_rz (Z-1, F) and gwb_mrz (M-1, Z-1, F) bin w by the final redshift at bin centres over the
+ * redz edges (scipy.stats.binned_statistic's rule); num_* are the same sums of number, undivided.
+ * n_mtot, n_mrat, n_redz are edge counts; redz_final is (M, Q, Z, F); redz_edges (Z) device. */
+int hgb_model_details(const double *number, const double *h2fdf, const double *redz_final, const double *redz_edges,
+                      int n_mtot, int n_mrat, int n_redz, int n_freq, double *gwb_m, double *gwb_q, double *gwb_z,
+                      double *gwb_rz, double *num_m, double *num_q, double *num_z, double *num_rz, double *gwb_mrz,
+                      double *num_mrz, double *denom, void *stream);
+
+/* No reference counterpart.  Measurement hook for the realization kernel: with enable != 0,
+ * hgb_loudest_hc_from_sorted (HGB_RNG_PHILOX) records CUDA events on its stream immediately
+ * before and after its bulk-background kernel, on the calling host thread.
+ * hgb_bulk_last_ms() returns the time between the last recorded pair in ms (call it after
+ * synchronising the stream), or -1 when nothing was recorded since hgb_bulk_timing(). */
+int hgb_bulk_timing(int enable);
+float hgb_bulk_last_ms(void);
 
 /* Second-pass GWB without the loudest split.  Replaces cyutils.sam_poisson_gwb,
  * cyutils.pyx:854-897; gwb is (F, R).  replay[(b*F + f)*R + r] in REPLAY mode (no workspace needed). */

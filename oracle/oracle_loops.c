@@ -269,3 +269,29 @@ void orc_fill_loudest(int nbins, const double *h2fdf_sorted, const double *num_s
 void orc_poisson_gwb_bin(int nreals, int ff, const double *num, double bin_hc2, double *gwb) {
     for (int rr = 0; rr < nreals; rr++) gwb[(long)ff * nreals + rr] += num[rr] * bin_hc2;
 }
+
+/* holodeck/cyutils.pyx:1700-1770 (_loudest_hc_and_par_from_sorted_redz), one (realization,
+ * frequency): bins in loudest-first order, `num_sorted` the draws, `par_sorted` the bin's
+ * parameters [7][nbins] (mt, mr, rz, redz_final, dcom_final, sepa, angs).  Writes hc2ss[nloud],
+ * sspar[4][nloud] (stride ss_stride between parameters), hc2bg and bgpar[7] (stride bg_stride). */
+void orc_fill_loudest_par(int nbins, const double *h2fdf_sorted, const double *num_sorted, const double *par_sorted,
+                          int nloud, double *hc2ss, double *sspar, long ss_stride, double *hc2bg, double *bgpar,
+                          long bg_stride) {
+    int ll = 0;
+    double sum_bg = 0, wsum[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int bb = 0; bb < nbins; bb++) {
+        double num = num_sorted[bb];
+        double cur = h2fdf_sorted[bb];
+        if ((num < 1) || (cur == 0)) continue;
+        while ((ll < nloud) && (num > 0)) {
+            hc2ss[ll] = cur;
+            for (int k = 0; k < 4; k++) sspar[k * ss_stride + ll] = par_sorted[(long)k * nbins + bb];
+            num -= 1;
+            ll += 1;
+        }
+        sum_bg += num * cur;
+        for (int k = 0; k < 7; k++) wsum[k] += num * cur * par_sorted[(long)k * nbins + bb];
+    }
+    *hc2bg = sum_bg;
+    for (int k = 0; k < 7; k++) bgpar[k * bg_stride] = wsum[k] / sum_bg;
+}

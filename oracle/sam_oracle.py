@@ -56,6 +56,7 @@ def lib():
         _LIB.orc_dbn_2pwl.argtypes = [p, i, d, i, p, d, d, d, p, p, i, p, i, p, i, p, p, p, p, i, p, p]
         _LIB.orc_dbn_gw.argtypes = [p, i, p, p, i, p, i, i, p, p, p, i, p, p]
         _LIB.orc_fill_loudest.argtypes = [i, p, p, i, p, p]
+        _LIB.orc_fill_loudest_par.argtypes = [i, p, p, p, i, p, p, ctypes.c_long, p, p, ctypes.c_long]
         _LIB.orc_hard_func_2pwl_gw.argtypes = [i, p, p, p, p, d, d, d, p]
     return _LIB
 
@@ -400,6 +401,106 @@ def ss_gws_redz(edges, redz, number, realize, loudest=1, seed=None, counts=None,
         raise Exception("`realize` must be an integer!")
     hc2ss, hc2bg = loudest_hc_from_sorted(number, h2fdf, realize, loudest, order, seed=seed, counts=counts)
     return np.sqrt(hc2ss), np.sqrt(hc2bg)
+
+
+def param_grids(edges, redz, cosmo=None):
+    """single_sources.py:117-143: bin-centre final redshift (-1 where <= 0), comoving distance
+    (+inf there), Kepler separation at the rest-frame orbital frequency, angular separation."""
+    cosmo = _cosmo if cosmo is None else cosmo
+    mt = midpoints(edges[0])
+    for dd in range(3):
+        redz = midpoints(redz, axis=dd)
+    redz = np.array(redz)
+    dcom = np.inf * np.ones_like(redz)
+    sel = redz > 0.0
+    redz[~sel] = -1.0
+    redz[redz < 0] = -1.0
+    dcom[sel] = cosmo.comoving_distance(redz[sel])
+    fobs_orb_cents = midpoints(edges[-1])
+    frst = fobs_orb_cents[np.newaxis, np.newaxis, np.newaxis, :] * (1.0 + redz)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        sepa = np.power(C.NWTG * mt[:, np.newaxis, np.newaxis, np.newaxis] / np.square(2.0 * np.pi * frst), 1.0 / 3.0)
+        angs = sepa / (dcom / (1.0 + redz))
+    return redz, dcom, sepa, angs
+
+
+def loudest_hc_and_par_from_sorted(number, h2fdf, nreals, nloudest, order, pars, seed=None, counts=None):
+    """cyutils.pyx:1541-1770: (hc2ss[F,R,L], hc2bg[F,R], sspar[4,F,R,L], bgpar[7,F,R]); ``pars`` is the
+    list of the seven (B, F) parameter grids (mt, mr, rz broadcast, redz, dcom, sepa, angs)."""
+    L = lib()
+    nf = number.shape[-1]
+    lam = _c64(number.reshape(-1, nf)[order].T)
+    hh = _c64(h2fdf.reshape(-1, nf)[order].T)
+    pp = _c64(np.stack([np.broadcast_to(p, number.shape).reshape(-1, nf)[order].T for p in pars], axis=1))  # (F,7,B)
+    nb = lam.shape[1]
+    hc2ss = np.zeros((nf, nreals, nloudest))
+    hc2bg = np.zeros((nf, nreals))
+    sspar = np.zeros((4, nf, nreals, nloudest))
+    bgpar = np.zeros((7, nf, nreals))
+    rng = None if counts is not None else np.random.Generator(np.random.PCG64(seed))
+    ss = np.zeros(nloudest)
+    sp = np.zeros((4, nloudest))
+    bg = np.zeros(1)
+    bp = np.zeros(7)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for rr in range(nreals):
+            for ff in range(nf):
+                num = _c64(counts[rr, ff] if counts is not None else draw_counts(rng, lam[ff]))
+                ss[:] = 0.0
+                sp[:] = 0.0
+                par = _c64(pp[ff])
+                L.orc_fill_loudest_par(nb, _ptr(hh[ff]), _ptr(num), _ptr(par), nloudest, _ptr(ss), _ptr(sp),
+                                       nloudest, _ptr(bg), _ptr(bp), 1)
+                hc2ss[ff, rr] = ss
+                hc2bg[ff, rr] = bg[0]
+                sspar[:, ff, rr] = sp
+                bgpar[:, ff, rr] = bp
+    return hc2ss, hc2bg, sspar, bgpar
+
+
+def ss_gws_redz_params(edges, redz, number, realize, loudest=1, seed=None, counts=None, cosmo=None):
+    """single_sources.py:40-174 (params=True branch): (hc_ss, hc_bg, sspar, bgpar)."""
+    h2fdf = char_strain_sq_from_bin_edges_redz(edges, redz, cosmo=cosmo)
+    order = sort_order(h2fdf)
+    if np.any(np.logical_and(redz < 0, redz != -1)):
+        raise ValueError(f"{np.sum(np.logical_and(redz < 0, redz != -1))} redz < 0 and !=-1 found in redz")
+    rz_m, dcom, sepa, angs = param_grids(edges, redz, cosmo=cosmo)
+    mt, mr, rz = midpoints(edges[0]), midpoints(edges[1]), midpoints(edges[2])
+    pars = [mt[:, None, None, None], mr[None, :, None, None], rz[None, None, :, None], rz_m, dcom, sepa, angs]
+    hc2ss, hc2bg, sspar, bgpar = loudest_hc_and_par_from_sorted(number, h2fdf, realize, loudest, order, pars,
+                                                                seed=seed, counts=counts)
+    return np.sqrt(hc2ss), np.sqrt(hc2bg), sspar, bgpar
+
+
+def calc_model_details(edges, redz_final, number, cosmo=None):
+    """lib_tools.py:845-943: strain-weighted and number marginals of mtot, mrat, redz and of the final
+    redshift at bin centres (binned on the redz edges with scipy.stats.binned_statistic)."""
+    redz = edges[2]
+    nm, nz, nf = len(edges[0]) - 1, len(redz) - 1, len(edges[3]) - 1
+    w = char_strain_sq_from_bin_edges_redz(edges, redz_final, cosmo=cosmo) * number
+    denom = np.sum(w, axis=(0, 1, 2))
+    gwb_pars, num_pars = [], []
+    for axes in [(1,), (0,), (0, 1)]:
+        gwb_pars.append(np.sum(w, axis=axes) / denom)
+        num_pars.append(np.sum(number, axis=axes))
+    rz = redz_final.copy()
+    for ii in range(3):
+        rz = midpoints(rz, axis=ii)
+    g_m, n_m = np.zeros((nm, nz, nf)), np.zeros((nm, nz, nf))
+    g_rz, n_rz = np.zeros((nz, nf)), np.zeros((nz, nf))
+    for ff in range(nf):
+        flat = rz[..., ff].flatten()
+        g_rz[:, ff] = scipy.stats.binned_statistic(flat, w[..., ff].flatten(), bins=redz, statistic='sum')[0] / denom[ff]
+        n_rz[:, ff] = scipy.stats.binned_statistic(flat, number[..., ff].flatten(), bins=redz, statistic='sum')[0]
+        for mm in range(nm):
+            flat = rz[mm, :, :, ff].flatten()
+            g_m[mm, :, ff] = scipy.stats.binned_statistic(flat, w[mm, :, :, ff].flatten(), bins=redz,
+                                                          statistic='sum')[0] / denom[ff]
+            n_m[mm, :, ff] = scipy.stats.binned_statistic(flat, number[mm, :, :, ff].flatten(), bins=redz,
+                                                          statistic='sum')[0]
+    gwb_pars.append(g_rz)
+    num_pars.append(n_rz)
+    return gwb_pars, num_pars, g_m, n_m
 
 
 def sam_poisson_gwb(number, hc2, nreals, seed, thresh=NORMAL_THRESHOLD):

@@ -171,6 +171,58 @@ def case_loudest_edges():
     save("ref_loudest_edges.npz", **out, ncases=3)
 
 
+def case_params():
+    """``ss_gws_redz(params=True)`` (single_sources.py:102-161 -> cyutils.pyx:1541-1770): loudest-source
+    parameters and background-weighted means, through ``gwb(params=True)`` as well."""
+    sam = make_sam((10, 11, 12), 0.0)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 5)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    fobs_orb_edges = fobs_gw_edges / 2.0
+    fobs_orb_cents = 0.5 * (fobs_gw_edges[1:] + fobs_gw_edges[:-1]) / 2.0
+    redz_final, dnum = sam_cyutils.dynamic_binary_number_at_fobs(fobs_orb_cents, sam, hard, holo.cosmo)
+    edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
+    number = sam_cyutils.integrate_differential_number_3dx1d(edges, dnum)
+    out = dict(mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, fobs_gw_edges=fobs_gw_edges,
+               fobs_orb_edges=fobs_orb_edges, redz_final=redz_final, number=number)
+    h2fdf = gravwaves.char_strain_sq_from_bin_edges_redz(edges, redz_final)
+    order = np.argsort(-h2fdf[..., 0].flatten())
+    lam = number.reshape(-1, number.shape[-1])[order]   # (B, F) in the reference's visiting order
+    for ii, (nreals, nloud, seed) in enumerate([(6, 3, 21), (2, 40, 22)]):
+        seed_rng(seed)
+        hc_ss, hc_bg, sspar, bgpar = single_sources.ss_gws_redz(edges, redz_final, number, realize=nreals,
+                                                                loudest=nloud, params=True)
+        # the draws the reference made (numpy's PCG64 stream in its visiting order; no Normal bins here),
+        # kept so that a replay does not depend on the numpy build of the machine that runs the test
+        assert np.all(lam <= 1e10)
+        rng = np.random.Generator(np.random.PCG64(seed))
+        counts = np.array([[rng.poisson(lam[:, ff]) for ff in range(lam.shape[1])] for _ in range(nreals)],
+                          dtype=np.float64)
+        out.update({f"c{ii}_nreals": nreals, f"c{ii}_nloud": nloud, f"c{ii}_seed": seed, f"c{ii}_hc_ss": hc_ss,
+                    f"c{ii}_hc_bg": hc_bg, f"c{ii}_sspar": sspar, f"c{ii}_bgpar": bgpar, f"c{ii}_counts": counts})
+    seed_rng(21)
+    g = sam.gwb(fobs_gw_edges, hard=hard, realize=6, loudest=3, params=True)
+    assert all(np.array_equal(a, b, equal_nan=True) for a, b in
+               zip(g, (out["c0_hc_ss"], out["c0_hc_bg"], out["c0_sspar"], out["c0_bgpar"])))
+    save("ref_params.npz", **out, ncases=2, hard_time=3.0 * GYR)
+
+
+def case_details():
+    """``_calc_model_details`` (librarian/lib_tools.py:845-943) and ``run_model``'s deterministic keys."""
+    from holodeck.librarian import lib_tools
+    sam = make_sam((10, 11, 12), 0.0)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    seed_rng(31)
+    data = lib_tools.run_model(sam, hard, nfreqs=6, nreals=4, nloudest=2, gwb_flag=False, singles_flag=True,
+                               details_flag=True, params_flag=False)
+    out = dict(mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, fobs_cents=data['fobs_cents'],
+               fobs_edges=data['fobs_edges'], number=data['number'], redz_final=data['redz_final'],
+               gwb_mtot_redz_final=data['gwb_mtot_redz_final'], num_mtot_redz_final=data['num_mtot_redz_final'])
+    for ii in range(4):
+        out[f"gwb_params_{ii}"] = data['gwb_params'][ii]
+        out[f"num_params_{ii}"] = data['num_params'][ii]
+    save("ref_details.npz", **out, hard_time=3.0 * GYR)
+
+
 def case_known_answers():
     """Known-answer values the reference pins for the strain formula (holodeck/tests/test_utils.py:52-96)."""
     path = os.path.join(ref_env.REF_SRC, "holodeck", "tests", "test_utils.py")
@@ -191,7 +243,10 @@ def case_known_answers():
          check_hs=holo.utils.gw_strain_source(vals["mc"], vals["dc"], freq))
 
 
-def main():
+def main(only=None):
+    if only:
+        globals()[only]()
+        return
     case_known_answers()
     case_loudest_edges()
     case_norm_sweep()
@@ -199,7 +254,9 @@ def main():
     case_small(0.28, "scatter")
     case_scatter_shapes()
     case_cfg1()
+    case_params()
+    case_details()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -235,7 +235,7 @@ def test_philox_poisson_statistics(built_lib):
     """Counts of the Philox sampler follow Poisson(lambda) across all sampler regimes."""
     from holodeck_gb300 import cyutils
     from scipy import stats
-    lams = np.array([1e-7, 0.03, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 9.1e4, 5.0e6])
+    lams = np.array([1e-7, 0.03, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 6.0e4, 9.1e4, 5.0e6])
     nreals = 20000
     # one bin per lambda, one frequency; L=0 so every source goes to the background sum
     number = lams.reshape(-1, 1, 1, 1)
@@ -305,3 +305,39 @@ def test_philox_matches_oracle_statistics(built_lib):
             pa, pb = np.percentile(np.sqrt(a), q), np.percentile(np.sqrt(b), q)
             assert abs(pa / pb - 1.0) < 0.03, (ff, q, pa, pb)
         assert abs(a.var() / b.var() - 1.0) < 0.25
+
+
+def test_philox_loudest_slots_distribution(built_lib):
+    """Which bins fill the loudest slots, and the background left over, follow the reference's
+    in-order walk: Philox realizations vs numpy-Poisson realizations of the oracle, two-sample
+    chi-square over the slot tuples and moments of the background."""
+    from holodeck_gb300 import cyutils
+    from scipy import stats
+    # sorted by h at the first frequency: bin k is the k-th loudest; lambdas cover every sampler
+    lams = np.array([0.2, 1e-3, 1.5, 0.01, 3.0, 0.6, 25.0, 7.0, 400.0])
+    hs = np.linspace(9.0, 1.0, lams.size) * 1e-30
+    number = lams.reshape(-1, 1, 1, 1)
+    h2fdf = hs.reshape(-1, 1, 1, 1)
+    ms, qs, zs = np.unravel_index(np.arange(lams.size), number.shape[:3])
+    nreals, nloud = 100_000, 3
+    ss, bg = cyutils.loudest_hc_from_sorted(number, h2fdf, nreals, nloud, ms, qs, zs, seed=31337)
+    ss_o, bg_o = O.loudest_hc_from_sorted(number, h2fdf, nreals, nloud, np.arange(lams.size), seed=4242)
+
+    def tuples(s):
+        idx = np.rint(s[0] / 1e-30).astype(np.int64)   # slot value -> 9..1, 0 when empty
+        return idx[:, 0] * 100 + idx[:, 1] * 10 + idx[:, 2]
+
+    ta, tb = tuples(ss), tuples(ss_o)
+    cats = np.union1d(ta, tb)
+    ca = np.array([(ta == c).sum() for c in cats])
+    cb = np.array([(tb == c).sum() for c in cats])
+    keep = (ca + cb) >= 20
+    chi2, p, _, _ = stats.chi2_contingency(np.stack([ca[keep], cb[keep]]))
+    assert p > 1e-4, (chi2, p, cats[keep], ca[keep], cb[keep])
+    # background: mean and variance against the oracle; total mean against sum(lambda h)
+    a, b = bg[0], bg_o[0]
+    se = np.sqrt(a.var() / nreals + b.var() / nreals)
+    assert abs(a.mean() - b.mean()) < 5 * se
+    assert abs(a.var() / b.var() - 1.0) < 0.05
+    tot = a + ss[0].sum(axis=-1)
+    assert abs(tot.mean() / (lams * hs).sum() - 1.0) < 5 * tot.std() / np.sqrt(nreals) / (lams * hs).sum()

@@ -94,3 +94,32 @@ def test_known_answer_strain():
     hs = utils.gw_strain_source(g["mc"], g["dc"], g["freq"])
     assert rel_err(hs, g["hs"]) < 1e-8
     assert np.allclose(hs, g["check_hs"], rtol=1e-14, atol=0)
+
+
+def test_oracle_params_path_bit_exact():
+    """ss_gws_redz(params=True): loudest-source parameters and background-weighted means
+    (single_sources.py:102-161, cyutils.pyx:1541-1770), replaying the reference's PCG64 stream."""
+    g = load_golden("ref_params.npz")
+    edges = [g["mtot"], g["mrat"], g["redz"], g["fobs_orb_edges"]]
+    h2 = O.char_strain_sq_from_bin_edges_redz(edges, g["redz_final"])
+    order = O.sort_order(h2)
+    for ii in range(int(g["ncases"])):
+        nreals, nloud, seed = int(g[f"c{ii}_nreals"]), int(g[f"c{ii}_nloud"]), int(g[f"c{ii}_seed"])
+        counts = O.replay_counts(g["number"], order, nreals, seed)
+        assert np.array_equal(counts, g[f"c{ii}_counts"])
+        out = O.ss_gws_redz_params(edges, g["redz_final"], g["number"], nreals, nloud, counts=counts)
+        for got, name in zip(out, ["hc_ss", "hc_bg", "sspar", "bgpar"]):
+            assert np.array_equal(got, g[f"c{ii}_{name}"], equal_nan=True), (ii, name)
+
+
+def test_oracle_model_details_bit_exact():
+    """_calc_model_details (librarian/lib_tools.py:845-943) on the reference's run_model output."""
+    g = load_golden("ref_details.npz")
+    fe = g["fobs_edges"] / 2.0
+    edges = [g["mtot"], g["mrat"], g["redz"], fe]
+    gwb_pars, num_pars, gm, nm = O.calc_model_details(edges, g["redz_final"], g["number"])
+    for ii in range(4):
+        assert np.array_equal(gwb_pars[ii], g[f"gwb_params_{ii}"]), ii
+        assert np.array_equal(num_pars[ii], g[f"num_params_{ii}"]), ii
+    assert np.array_equal(gm, g["gwb_mtot_redz_final"])
+    assert np.array_equal(nm, g["num_mtot_redz_final"])
