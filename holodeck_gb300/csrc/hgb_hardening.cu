@@ -6,7 +6,9 @@
 //    per starting redshift, step tables in shared memory) and records, per target frequency, the
 //    interpolated time of the bracketing step; k_dbn_2pwl_eval then evaluates redshift, distance,
 //    residence time and number for every bracketed (redz, frequency) element in parallel, with the
-//    model's (half-)integer exponents taken as products and square roots instead of pow().
+//    model's (half-)integer exponents taken as products and square roots instead of pow().  The
+//    age -> redshift / distance interpolations use per-interval slopes computed once per block
+//    (a multiply instead of a divide per lookup; results differ from the reference's divide by an ulp).
 //  * hgb_dbn_gw: differential binary number for Hard_GW (sam_cyutils.pyx:788-899); one thread per
 //    grid point.
 // FP64 throughout (the hardening integral and the lookback-time -> redshift inversion are the
@@ -218,6 +220,7 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
     double *dadt = frst + (S + 1);   // [S+1]
     double *dts = dadt + (S + 1);    // [S]
     double *tevo = dts + S;          // [S]
+    double *sz = tevo + S;           // [NI] dz/dt of each age-table interval
 
     int cell = blockIdx.x;
     int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
@@ -230,6 +233,8 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
         dg[i] = dgrid_g[i];
     }
     for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = fobs[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < NI - 1; i += blockDim.x) sz[i] = (zg[i + 1] - zg[i]) / (ag[i + 1] - ag[i]);
     double risco = 3.0 * HGB_CY_SCHW * mt;
     double dx = (a.sepa_init_log10 - log10(risco)) / S;
     if (threadIdx.x == 0) {
@@ -315,12 +320,12 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
                 redz_left = prev_zr;
             } else {
                 il = hgb::while_while_increasing(il, NI, time_left, ag);
-                redz_left = hgb::interp_between(time_left, ag[il], ag[il + 1], zg[il], zg[il + 1]);
+                redz_left = zg[il] + (time_left - ag[il]) * sz[il];
             }
             if (redz_left < 0.0) continue;
             fl = reuse ? prev_fr : frst[s] / (1.0 + redz_left);
             int ir = hgb::while_while_increasing(il, NI, time_right, ag);
-            double redz_right = hgb::interp_between(time_right, ag[ir], ag[ir + 1], zg[ir], zg[ir + 1]);
+            double redz_right = zg[ir] + (time_right - ag[ir]) * sz[ir];
             double zr_raw = redz_right;
             if (redz_right < 0.0) redz_right = 0.0;
             double fr = frst[s + 1] / (1.0 + redz_right);
@@ -372,6 +377,8 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
     double *ag = zg + NI;
     double *dg = ag + NI;
     double *ft = dg + NI;
+    double *sz = ft + NF;            // [NI] dz/dt and d(d_C)/dt of each age-table interval
+    double *sd = sz + NI;
     const int cell = blockIdx.x;
     const int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
     for (int i = threadIdx.x; i < NI; i += blockDim.x) {
@@ -380,6 +387,12 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
         dg[i] = dgrid_g[i];
     }
     for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = fobs[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < NI - 1; i += blockDim.x) {
+        const double dt = ag[i + 1] - ag[i];
+        sz[i] = (zg[i + 1] - zg[i]) / dt;
+        sd[i] = (dg[i + 1] - dg[i]) / dt;
+    }
     __shared__ double s_mt3, s_mr12, s_mt13;
     const double mt = mtot[ii], mr = mrat[jj], norm = hard_norm[cell];
     if (threadIdx.x == 0) {
@@ -398,8 +411,8 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
         const int kk = (int)(e / NF);
         const double new_time = diff_num[base + e];
         int ni = hgb::while_while_increasing((int)hint, NI, new_time, ag);
-        double new_redz = hgb::interp_between(new_time, ag[ni], ag[ni + 1], zg[ni], zg[ni + 1]);
-        double dcom = hgb::interp_between(new_time, ag[ni], ag[ni + 1], dg[ni], dg[ni + 1]);
+        double new_redz = zg[ni] + (new_time - ag[ni]) * sz[ni];
+        double dcom = dg[ni] + (new_time - ag[ni]) * sd[ni];
         double target_frst_orb = ft[f] * (1.0 + new_redz);
         const double cb = cbrt(target_frst_orb);   // target^(2/3) as cbrt(target)^2
         double sp = cc.ksepa * mt13 / (cb * cb);
@@ -708,7 +721,7 @@ int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sep
     Dbn2plArgs a{log10(sepa_init), rchar, gamma_inner, gamma_outer, num_steps, n_freq, fobs_sorted ? 1 : 0,
                  n_mtot, n_mrat, n_redz, cosmo->grid_size, pow_plan(-gamma_outer + gamma_inner),
                  pow_plan(gamma_inner - 1.0)};
-    size_t smem = sizeof(double) * ((size_t)3 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
+    size_t smem = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
                                     2 * (size_t)num_steps);
     HGB_CHECK_ARG(smem <= 200 * 1024);
     if (smem > 48 * 1024) {
@@ -727,7 +740,7 @@ int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sep
                                                                 diff_num);
     int rc = hgb::check_launch();
     if (rc) return rc;
-    size_t smem2 = sizeof(double) * ((size_t)3 * cosmo->grid_size + n_freq);
+    size_t smem2 = sizeof(double) * ((size_t)5 * cosmo->grid_size + n_freq);
     k_dbn_2pwl_eval<<<blocks, 256, smem2, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden, mtot,
                                                                   mrat, cosmo->grid_z, cosmo->grid_age,
                                                                   cosmo->grid_dcom, redz_final, diff_num);

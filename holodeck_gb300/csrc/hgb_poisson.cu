@@ -79,8 +79,9 @@ constexpr int MAX_PREFIX_EXTRA = 1024;   // prefix events beyond L (Normal draws
 constexpr double TABLE_MAX = 65536.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 9
 constexpr int TMAX = 4096;               // table entries (>= 14 * 256 + 9)
 constexpr int ARENA_WORDS = TMAX + TMAX / 2;   // one largest table: cdf words + u16 guide cells
+constexpr int HALF_WORDS = ARENA_WORDS / 2;   // the arena's halves alternate between build and draw
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
-constexpr int TABLE_WARP_MAX = 1024;     // larger tables are built by the whole block
+constexpr int ANCHOR = 8;                // Loader-form pmf every ANCHOR-th entry, the recursion between
 constexpr float TABLE_SIGMAS = 7.0f;     // the table covers lambda +- 7 sqrt(lambda) (tails < 1e-11)
 // draw families (counter .w high bits)
 constexpr uint32_t W_SMALL = 0x00000000u;   // | call: 4 realizations per call
@@ -234,7 +235,7 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
             const int S = min((int)ceilf(lf + TABLE_SIGMAS * sd + 6.0f) - k_lo + 1, TMAX);
             s.tb_klo[j] = k_lo;
             s.tb_S[j] = S;
-            s.tb_gb[j] = 32 - __clz(S - 1);   // ceil(log2 S), S >= 2
+            s.tb_gb[j] = 32 - __clz(S - 1);   // ceil(log2 S): 2^gb >= S guide cells, S >= 2
         }
         if (kind == KIND_PTRS32) {
             const float slam = sqrtf(lf);
@@ -657,10 +658,11 @@ struct BulkArgs {
 };
 
 // Builds the inversion table of one table-kind bin (lambda in [10, TABLE_MAX]) with one warp:
-// P(k) for k = k_lo .. k_lo + S - 1 in FP32 (the Loader form at every fourth entry, the recursion
+// P(k) for k = k_lo .. k_lo + S - 1 in FP32 (the Loader form at every ANCHOR-th entry, the recursion
 // P(k) = P(k-1) lambda / k in between), rounded to 32.32 fixed point, summed exactly in integers
-// (warp scan) into cdf[m] = floor(CDF 2^32), and the guide cells 2^gb >= S: guide[i] = smallest m
-// with cdf[m] > i 2^(32 - gb).  The mass outside the range (< 1e-11) goes to the end entries.
+// (warp scan) into cdf[m] = floor(CDF 2^32), and 2^gb >= S guide cells:
+// guide[i] = smallest m with cdf[m] > i 2^(32 - gb).  The mass outside the range (< 1e-11) goes to
+// the end entries.
 __device__ void build_table_warp(const Tile &s, int j, unsigned int *cdf, unsigned short *guide, int lane) {
     const int S = s.tb_S[j], k_lo = s.tb_klo[j], shift = 32 - s.tb_gb[j];
     const int E = (S + 31) >> 5;
@@ -671,8 +673,8 @@ __device__ void build_table_warp(const Tile &s, int j, unsigned int *cdf, unsign
     float p = 0.0f;
     for (int m = m0; m < m1; m++) {
         const int k = k_lo + m;
-        if (((m - m0) & 3) == 0) p = pmf_f32(k, lam_int, frac, lamf);
-        else p = __fdividef(p * lamf, (float)k);   // 2 ulp per step, three steps per anchor
+        if (((m - m0) & (ANCHOR - 1)) == 0) p = pmf_f32(k, lam_int, frac, lamf);
+        else p = p * lamf / (float)k;   // correctly rounded steps: < 4 ulp drift before the next anchor
         const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
         cdf[m] = qm;
         local += qm;
@@ -712,8 +714,8 @@ __device__ void build_table_block(Tile &s, int j, unsigned int *cdf, unsigned sh
     float p = 0.0f;
     for (int m = m0; m < m1; m++) {
         const int k = k_lo + m;
-        if (((m - m0) & 3) == 0) p = pmf_f32(k, lam_int, frac, lamf);
-        else p = __fdividef(p * lamf, (float)k);
+        if (((m - m0) & (ANCHOR - 1)) == 0) p = pmf_f32(k, lam_int, frac, lamf);
+        else p = p * lamf / (float)k;
         const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
         cdf[m] = qm;
         local += qm;
@@ -898,75 +900,121 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
             }
         }
 
-        // ---- table kind: inversion tables of up to BATCH_MAX bins at a time, packed in the arena and
-        // built one per warp; four realizations per Philox call
+        // ---- table kind: inversion tables of up to BATCH_MAX bins at a time.  Tables that fit half the
+        // arena are built one per warp into the half the draws are not reading: batch k + 1 is built
+        // while batch k is drawn, one barrier per batch.  Larger tables use the whole arena and the
+        // whole block.  Four realizations per Philox call.
         const int n_table = kind_count(s, KIND_TABLE);
-#pragma unroll 1
-        for (int li = 0; li < n_table;) {
-            // the batch (same on every thread): one large table, or up to BATCH_MAX small ones
-            const bool big = s.tb_S[s.list[KIND_TABLE][li]] > TABLE_WARP_MAX;
-            int K = 0, used = 0;
-            while (li + K < n_table && K < BATCH_MAX) {
-                const int jj = s.list[KIND_TABLE][li + K];
-                const int words = table_words(s, jj);
-                if (K > 0 && (big || s.tb_S[jj] > TABLE_WARP_MAX || used + words > ARENA_WORDS)) break;
-                used += words;
-                K++;
-            }
-            __syncthreads();   // the arena is free (previous batch, or the small-lambda pass)
-            if (big) {
-                const int j = s.list[KIND_TABLE][li];
-                build_table_block(s, j, s.u.arena, (unsigned short *)(s.u.arena + s.tb_S[j]));
-            } else {
-                // each table to the least-loaded warp so far (by entries), lowest warp on ties
+        if (n_table > 0) {
+            int li = 0;
+            int cur_li = 0, cur_K = 0, cur_half = 0;
+            bool cur_big = false;
+            // the batch starting at list entry li (same on every thread)
+            auto form = [&](int at, int &K, bool &big) {
+                big = table_words(s, s.list[KIND_TABLE][at]) > HALF_WORDS;
+                K = 1;
+                if (big) return;
+                int used = table_words(s, s.list[KIND_TABLE][at]);
+                while (at + K < n_table && K < BATCH_MAX) {
+                    const int words = table_words(s, s.list[KIND_TABLE][at + K]);
+                    if (words > HALF_WORDS || used + words > HALF_WORDS) break;
+                    used += words;
+                    K++;
+                }
+            };
+            // build a small batch into a half, each table by the least-loaded warp (by entries)
+            auto build_small = [&](int at, int K, int half) {
                 int load[NWARP] = {};
-                int off = 0;
+                int off = half * HALF_WORDS;
                 for (int i = 0; i < K; i++) {
-                    const int j = s.list[KIND_TABLE][li + i];
+                    const int j = s.list[KIND_TABLE][at + i];
                     int wmin = 0;
 #pragma unroll
                     for (int w = 1; w < NWARP; w++)
                         if (load[w] < load[wmin]) wmin = w;
                     load[wmin] += s.tb_S[j];
                     if (wmin == warp)
-                        build_table_warp(s, j, s.u.arena + off, (unsigned short *)(s.u.arena + off + s.tb_S[j]),
-                                         lane);
+                        build_table_warp(s, j, s.u.arena + off, (unsigned short *)(s.u.arena + off + s.tb_S[j]), lane);
                     off += table_words(s, j);
                 }
-                __syncthreads();   // every table of the batch is ready
+            };
+            form(li, cur_K, cur_big);
+            cur_li = li;
+            li += cur_K;
+            __syncthreads();   // the arena is free (the small-lambda pass is done)
+            if (cur_big) {
+                const int j = s.list[KIND_TABLE][cur_li];
+                build_table_block(s, j, s.u.arena, (unsigned short *)(s.u.arena + s.tb_S[j]));
+            } else {
+                build_small(cur_li, cur_K, 0);
+                __syncthreads();
             }
-            int off = 0;
 #pragma unroll 1
-            for (int i = 0; i < K; i++) {
-                const int j = s.list[KIND_TABLE][li + i];
-                const int pos = s.pos[j];
-                const float hs = s.hs[j];
-                const int k_lo = s.tb_klo[j], S = s.tb_S[j], shift = 32 - s.tb_gb[j];
-                const unsigned int *cdf = s.u.arena + off;
-                const unsigned short *guide = (const unsigned short *)(s.u.arena + off + S);
-                off += table_words(s, j);
+            while (true) {
+                // prebuild the next batch when both it and the current one are small
+                int nxt_li = li, nxt_K = 0;
+                bool nxt_big = false;
+                if (!cur_big && li < n_table) {
+                    form(li, nxt_K, nxt_big);
+                    if (nxt_big) nxt_K = 0;
+                    else {
+                        li += nxt_K;
+                        build_small(nxt_li, nxt_K, cur_half ^ 1);
+                    }
+                }
+                // draw the current batch
+                int off = cur_big ? 0 : cur_half * HALF_WORDS;
+#pragma unroll 1
+                for (int i = 0; i < cur_K; i++) {
+                    const int j = s.list[KIND_TABLE][cur_li + i];
+                    const int pos = s.pos[j];
+                    const float hs = s.hs[j];
+                    const int k_lo = s.tb_klo[j], S = s.tb_S[j], shift = 32 - s.tb_gb[j];
+                    const unsigned int *cdf = s.u.arena + off;
+                    const unsigned short *guide = (const unsigned short *)(s.u.arena + off + S);
+                    off += table_words(s, j);
 #pragma unroll
-                for (int call = 0; call < RPT / 4; call++) {
-                    if (4 * call >= rpt) break;
-                    uint4 ctr = ctr0;
-                    ctr.x = (uint32_t)pos;
-                    ctr.w |= W_TABLE | (uint32_t)call;
-                    const uint4 w = philox(ctr, a.key);
+                    for (int call = 0; call < RPT / 4; call++) {
+                        if (4 * call >= rpt) break;
+                        uint4 ctr = ctr0;
+                        ctr.x = (uint32_t)pos;
+                        ctr.w |= W_TABLE | (uint32_t)call;
+                        const uint4 w = philox(ctr, a.key);
 #pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        const int sl = 4 * call + m;
-                        const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
-                        if (sl >= rpt) continue;
-                        int e = guide[u >> shift];
-                        while (e < S - 1 && u >= cdf[e]) e++;
-                        if (!check || pos >= __ldg(q_row + sl * RB)) {
-                            kahan_add(acc_r[sl], comp_r[sl], (float)(k_lo + e) * hs);
-                            if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + e));
+                        for (int m = 0; m < 4; m++) {
+                            const int sl = 4 * call + m;
+                            const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
+                            if (sl >= rpt) continue;
+                            int e = guide[u >> shift];
+                            while (e < S - 1 && u >= cdf[e]) e++;
+                            if (!check || pos >= __ldg(q_row + sl * RB)) {
+                                kahan_add(acc_r[sl], comp_r[sl], (float)(k_lo + e) * hs);
+                                if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + e));
+                            }
                         }
                     }
                 }
+                __syncthreads();   // the current batch is drawn and the next one built
+                if (nxt_K > 0) {
+                    cur_li = nxt_li;
+                    cur_K = nxt_K;
+                    cur_big = false;
+                    cur_half ^= 1;
+                    continue;
+                }
+                if (li >= n_table) break;
+                form(li, cur_K, cur_big);
+                cur_li = li;
+                li += cur_K;
+                if (cur_big) {
+                    const int j = s.list[KIND_TABLE][cur_li];
+                    build_table_block(s, j, s.u.arena, (unsigned short *)(s.u.arena + s.tb_S[j]));
+                } else {
+                    cur_half = 0;
+                    build_small(cur_li, cur_K, 0);
+                    __syncthreads();
+                }
             }
-            li += K;
         }
 
         // ---- PTRS32: one loop per lane over its realizations, two attempts per Philox call

@@ -79,13 +79,16 @@ __global__ void k_gradients(hgb_scatter_plan P, const double *__restrict__ dens,
 }
 
 // The same solve with the slice's values and gradients in shared memory, indexed by level-order
-// position (a level's points are contiguous), for grids whose state fits on one SM.  One warp per
-// slice: a level's points (about 20 at 91x81) share the warp's lanes, because the SM's FP64 pipe
-// costs the same per warp instruction however many lanes are active.  The static neighbour data of
-// the next level (first LV_REG edges of each point, and its inverse normal matrix) is loaded into
-// registers while the current level computes, so a level waits only on shared memory.  Operations
-// and their order are those of k_gradients.
-constexpr int LV_REG = 6;   // interior points of the triangulated grid have 6 neighbours
+// position (a level's points are contiguous), for grids whose state fits on one SM.  GB300's FP64
+// units belong to the four SM sub-partitions and charge each warp instruction in full however few
+// lanes are active, so the block has four warps, one per sub-partition: a level's points (about 20
+// at 91x81) share the lanes of every warp, warp w sums the terms of edges w, w+4, w+8, ... of its
+// point, and warp 0 adds the four partial sums and updates the point.  The static data of the next
+// level (each warp's first LV_REG edges of its point, warp 0's inverse normal matrix) is loaded into
+// registers while the current level computes.  Per point the terms are those of k_gradients; only
+// the grouping of the neighbour sum differs (four interleaved partial sums).
+constexpr int LV_WARPS = 4;
+constexpr int LV_REG = 3;   // edges w, w+4, w+8 per warp: interior points have 6 neighbours
 
 struct LvPre {
     int e0, e1;
@@ -94,35 +97,38 @@ struct LvPre {
     double2 q01, q23;
 };
 
-__device__ __forceinline__ void lv_load(const hgb_scatter_plan &P, const int *eptr, int p, bool active, LvPre &x) {
+__device__ __forceinline__ void lv_load(const hgb_scatter_plan &P, const int *eptr, int p, bool active, int warp,
+                                        LvPre &x) {
     x.e0 = active ? eptr[p] : 0;
     x.e1 = active ? eptr[p + 1] : 0;
 #pragma unroll
     for (int k = 0; k < LV_REG; k++) {
-        if (x.e0 + k < x.e1) {
-            const long e = x.e0 + k;
+        const int e = x.e0 + warp + LV_WARPS * k;
+        if (e < x.e1) {
             x.idx[k] = __ldg(P.lv_nbr + e);
-            x.w01[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * e));
-            x.w23[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * e + 2));
+            x.w01[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
+            x.w23[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
         }
     }
-    if (active) {
+    if (active && warp == 0) {
         x.q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
         x.q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
     }
 }
 
-__global__ void __launch_bounds__(32, 1) k_gradients_lv(hgb_scatter_plan P, const double *__restrict__ dens,
-                                                        int nz, double *__restrict__ vals,
-                                                        double *__restrict__ grads, int *d_status) {
+__global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_plan P, const double *__restrict__ dens,
+                                                                  int nz, double *__restrict__ vals,
+                                                                  double *__restrict__ grads, int *d_status) {
     extern __shared__ double sm[];
-    const int z = blockIdx.x, t = threadIdx.x;
+    __shared__ double psx[LV_WARPS][32], psy[LV_WARPS][32];
+    __shared__ int s_over;
+    const int z = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int n = P.n_mtot * P.n_mrat;
     double *f = sm;                                  // [n]
     double *g = f + n;                               // [n][2]
     int *eptr = (int *)(g + 2 * n);                  // [n + 1]
     int *lptr = eptr + n + 1;                        // [n_levels + 1]
-    for (int p = t; p < n; p += 32) {
+    for (int p = t; p < n; p += blockDim.x) {
         const int i = P.level_vtx[p];
         const double v = dens[(long)i * nz + z];
         f[p] = v;
@@ -132,75 +138,92 @@ __global__ void __launch_bounds__(32, 1) k_gradients_lv(hgb_scatter_plan P, cons
         eptr[p] = P.lv_nbr_ptr[p];
     }
     if (t == 0) eptr[n] = P.lv_nbr_ptr[n];
-    for (int l = t; l <= P.n_levels; l += 32) lptr[l] = P.level_ptr[l];
-    __syncwarp();
+    for (int l = t; l <= P.n_levels; l += blockDim.x) lptr[l] = P.level_ptr[l];
+    __syncthreads();
     const int nlev = P.n_levels;
     const double tol_lo = P.grad_tol * (1.0 - 1e-12);   // below this multiple of the scale: surely < tol
     bool converged = false;
     LvPre nxt;
-    lv_load(P, eptr, lptr[0] + t, t < lptr[1] - lptr[0], nxt);
+    lv_load(P, eptr, lptr[0] + lane, lane < lptr[1] - lptr[0], warp, nxt);
     for (int it = 0; it < P.grad_maxiter; it++) {
-        bool over = false;   // some point changed by >= grad_tol (relative) in this sweep
+        bool over = false;   // (warp 0) some point changed by >= grad_tol (relative) in this sweep
         for (int lev = 0; lev < nlev; lev++) {
             const int p0 = lptr[lev], p1 = lptr[lev + 1];
             const LvPre cur = nxt;
             {   // the next level (the first level again after the last), loaded ahead
                 const int nl = (lev + 1 < nlev) ? lev + 1 : 0;
                 const int q0 = lptr[nl], q1 = lptr[nl + 1];
-                lv_load(P, eptr, q0 + t, t < q1 - q0, nxt);
+                lv_load(P, eptr, q0 + lane, lane < q1 - q0, warp, nxt);
             }
-            for (int p = p0 + t; p < p1; p += 32) {
-                const bool pre = (p == p0 + t);   // the prefetched slot; wider levels load directly
-                const double fi = f[p];
+            for (int c0 = p0; c0 < p1; c0 += 32) {   // 32 points at a time (one pass at 91x81)
+                const int p = c0 + lane;
+                const bool act = p < p1;
+                const bool pre = (c0 == p0);         // the prefetched chunk; wider levels load directly
                 double sx = 0.0, sy = 0.0;
-                const int e0 = pre ? cur.e0 : eptr[p], e1 = pre ? cur.e1 : eptr[p + 1];
-                int e = e0;
-                if (pre) {
+                if (act) {
+                    const double fi = f[p];
+                    const int e0 = pre ? cur.e0 : eptr[p], e1 = pre ? cur.e1 : eptr[p + 1];
+                    int e = e0 + warp;
+                    if (pre) {
 #pragma unroll
-                    for (int k = 0; k < LV_REG; k++) {
-                        if (e0 + k < e1) {
-                            const int j = cur.idx[k];
-                            const double c =
-                                6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * cur.w01[k].x + g[2 * j + 1] * cur.w01[k].y);
-                            sx += c * cur.w23[k].x;
-                            sy += c * cur.w23[k].y;
+                        for (int k = 0; k < LV_REG; k++) {
+                            if (e < e1) {
+                                const int j = cur.idx[k];
+                                const double cc = 6.0 * (f[j] - fi) -
+                                                  2.0 * (g[2 * j] * cur.w01[k].x + g[2 * j + 1] * cur.w01[k].y);
+                                sx += cc * cur.w23[k].x;
+                                sy += cc * cur.w23[k].y;
+                            }
+                            e += LV_WARPS;
                         }
                     }
-                    e = e0 + LV_REG;
+                    for (; e < e1; e += LV_WARPS) {
+                        const int j = __ldg(P.lv_nbr + e);
+                        const double2 w01 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
+                        const double2 w23 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
+                        const double cc = 6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * w01.x + g[2 * j + 1] * w01.y);
+                        sx += cc * w23.x;
+                        sy += cc * w23.y;
+                    }
                 }
-                for (; e < e1; e++) {
-                    const int j = __ldg(P.lv_nbr + e);
-                    const double2 w01 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
-                    const double2 w23 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
-                    const double c = 6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * w01.x + g[2 * j + 1] * w01.y);
-                    sx += c * w23.x;
-                    sy += c * w23.y;
+                psx[warp][lane] = sx;
+                psy[warp][lane] = sy;
+                __syncthreads();
+                if (warp == 0 && act) {
+                    const double tx = ((psx[0][lane] + psx[1][lane]) + psx[2][lane]) + psx[3][lane];
+                    const double ty = ((psy[0][lane] + psy[1][lane]) + psy[2][lane]) + psy[3][lane];
+                    double2 q01, q23;
+                    if (pre) {
+                        q01 = cur.q01;
+                        q23 = cur.q23;
+                    } else {
+                        q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
+                        q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
+                    }
+                    const double nx = q01.x * tx + q01.y * ty;
+                    const double ny = q23.x * tx + q23.y * ty;
+                    // relative change, divided out only where the comparison with the tolerance is
+                    // close (the decision is that of change / scale < tol)
+                    const double change = fmax(fabs(nx - g[2 * p]), fabs(ny - g[2 * p + 1]));
+                    const double scale = fmax(1.0, fmax(fabs(nx), fabs(ny)));
+                    g[2 * p] = nx;
+                    g[2 * p + 1] = ny;
+                    if (change >= tol_lo * scale) over = over || (change / scale >= P.grad_tol);
                 }
-                double2 q01, q23;
-                if (pre) {
-                    q01 = cur.q01;
-                    q23 = cur.q23;
-                } else {
-                    q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
-                    q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
-                }
-                const double nx = q01.x * sx + q01.y * sy;
-                const double ny = q23.x * sx + q23.y * sy;
-                // relative change, divided out only where the comparison with the tolerance is
-                // close (the decision is that of change / scale < tol)
-                const double change = fmax(fabs(nx - g[2 * p]), fabs(ny - g[2 * p + 1]));
-                const double scale = fmax(1.0, fmax(fabs(nx), fabs(ny)));
-                g[2 * p] = nx;
-                g[2 * p + 1] = ny;
-                if (change >= tol_lo * scale) over = over || (change / scale >= P.grad_tol);
+                __syncthreads();
             }
-            __syncwarp();
         }
-        converged = !__any_sync(0xffffffffu, over);
+        if (warp == 0) {
+            const bool any = __any_sync(0xffffffffu, over);
+            if (lane == 0) s_over = any ? 1 : 0;
+        }
+        __syncthreads();
+        converged = (s_over == 0);
+        __syncthreads();
         if (converged) break;
     }
     if (!converged && t == 0) hgb::flag(d_status, HGB_STATUS_GRADIENT_NOT_CONVERGED);
-    for (int p = t; p < n; p += 32) {
+    for (int p = t; p < n; p += blockDim.x) {
         const int i = P.level_vtx[p];
         grads[2L * z * n + 2 * i] = g[2 * p];
         grads[2L * z * n + 2 * i + 1] = g[2 * p + 1];
@@ -284,7 +307,8 @@ __global__ void k_clough_tocher(hgb_scatter_plan P, const double *__restrict__ v
 }
 
 // ---- 3+4. redistribution and bilinear interpolation back to the points, as one dot product per
-// (point, slice): out = sum_j bw_i[j] ((1 - ty) G[j][b] + ty G[j][b + 1]); one warp per output.
+// (point, slice): out = sum_j bw_i[j] ((1 - ty) G[j][b] + ty G[j][b + 1]), with the two weight rows
+// (1 - ty) bw_i and ty bw_i precomputed, two fused multiply-adds per element; one warp per output.
 __global__ void k_back_dot(hgb_scatter_plan P, const double *__restrict__ gridT, int nz, double *__restrict__ dens) {
     const int n = P.n_mtot * P.n_mrat;
     const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -293,12 +317,12 @@ __global__ void k_back_dot(hgb_scatter_plan P, const double *__restrict__ gridT,
     const int i = (int)(warp / nz), z = (int)(warp % nz);
     const long N = P.n_grid;
     const int b = P.back_idx[2 * i + 1];
-    const double ty = P.back_t[2 * i + 1];
     const double *row0 = gridT + (long)z * N * N + (long)b * N;
     const double *row1 = row0 + N;
-    const double *bw = P.back_w + (long)i * N;
+    const double *w0 = P.back_w + 2L * i * N;   // (1 - ty) bw_i
+    const double *w1 = w0 + N;                 // ty bw_i
     double acc = 0.0;
-    for (int j = lane; j < N; j += 32) acc += bw[j] * ((1.0 - ty) * row0[j] + ty * row1[j]);
+    for (int j = lane; j < N; j += 32) acc = __fma_rn(w0[j], row0[j], __fma_rn(w1[j], row1[j], acc));
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) dens[(long)i * nz + z] = acc;
 }
@@ -339,9 +363,9 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     int dev = 0, smem_optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 64 <= (size_t)smem_optin) {
+    if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 4096 <= (size_t)smem_optin) {
         cudaFuncSetAttribute(k_gradients_lv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_smem);
-        k_gradients_lv<<<n_redz, 32, lv_smem, st>>>(P, dens, n_redz, vals, grads, d_status);
+        k_gradients_lv<<<n_redz, 32 * LV_WARPS, lv_smem, st>>>(P, dens, n_redz, vals, grads, d_status);
     } else {
         k_gradients<<<n_redz, 256, 0, st>>>(P, dens, n_redz, vals, grads, d_status);
     }

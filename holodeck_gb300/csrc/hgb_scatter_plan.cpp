@@ -579,12 +579,17 @@ int hgb_scatter_plan_build(const double *mtot, int n_mtot, const double *mrat, i
                 double *out = W2.data() + (long)j * N;
                 for (int a = 0; a < N; a++) out[a] += wjk * wk[a];
             }
+        // with the secondary-axis weights folded in: w0 = (1 - ty) bw_i, w1 = ty bw_i
         for (int i = 0; i < n; i++) {
             int a = plan->back_idx[2 * i];
-            double tx = plan->back_t[2 * i];
-            double *row = plan->back_w + (long)i * N;
-            for (int j = 0; j < N; j++)
-                row[j] = (1.0 - tx) * W2[(long)j * N + a] + tx * W2[(long)j * N + a + 1];
+            double tx = plan->back_t[2 * i], ty = plan->back_t[2 * i + 1];
+            double *row0 = plan->back_w + 2L * i * N;
+            double *row1 = row0 + N;
+            for (int j = 0; j < N; j++) {
+                const double bw = (1.0 - tx) * W2[(long)j * N + a] + tx * W2[(long)j * N + a + 1];
+                row0[j] = (1.0 - ty) * bw;
+                row1[j] = ty * bw;
+            }
         }
     }
 

@@ -40,7 +40,7 @@ def host_plan(mtot, mrat, scatter, refine=4):
                   nbr_idx=(nnbr,), nbr_w=(nnbr, 4), level_ptr=(nlev + 1,), level_vtx=(npts,),
                   grid_tri=(ngrid * ngrid,), grid_bary=(ngrid * ngrid, 3), grid_near=(ngrid * ngrid,),
                   grid_axis=(ngrid,), weights=(ngrid, ngrid), back_idx=(npts, 2), back_t=(npts, 2),
-                  back_w=(npts, ngrid), lv_nbr_ptr=(npts + 1,), lv_nbr=(nnbr,), lv_nbr_w=(nnbr, 4), lv_qinv=(npts, 4))
+                  back_w=(npts, 2, ngrid), lv_nbr_ptr=(npts + 1,), lv_nbr=(nnbr,), lv_nbr_w=(nnbr, 4), lv_qinv=(npts, 4))
     arrs = {kk: np.zeros(shapes[kk], dtype=_DTYPES[kk]) for kk in N._SCATTER_ARRAYS}
     hp = N.HgbScatterHostPlan(**{kk: arrs[kk].ctypes.data_as(ctypes.c_void_p) for kk in N._SCATTER_ARRAYS})
     sz = N.HgbScatterSizes()

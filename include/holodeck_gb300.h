@@ -140,7 +140,7 @@ typedef struct {    /* host arrays, sized by hgb_scatter_plan_bounds */
     double *weights;    /* [n_grid][n_grid] W[source][target] */
     int32_t *back_idx;  /* [n_pts][2] lower grid cell */
     double *back_t;     /* [n_pts][2] fractional offsets */
-    double *back_w;     /* [n_pts][n_grid] (1-tx) (W W)[:, a] + tx (W W)[:, a+1] */
+    double *back_w;     /* [n_pts][2][n_grid] (1-ty) bw and ty bw, bw = (1-tx) (W W)[:, a] + tx (W W)[:, a+1] */
     /* the neighbourhoods again, indexed by level-order position p (point level_vtx[p]) */
     int32_t *lv_nbr_ptr; /* [n_pts+1] */
     int32_t *lv_nbr;    /* [n_nbr] neighbour positions, in the order of nbr_idx */
