@@ -106,6 +106,7 @@ SIGNATURES = [
     ("hgb_argsort_f0_desc_static", _i, [_p, _l, _i, _p, _p]),
     ("hgb_loudest_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
     ("hgb_loudest_hc_from_sorted", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p]),
+    ("hgb_loudest_hc_from_sorted_ex", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p, _i]),
     ("hgb_param_grids", _i, [_p, _i, _i, _i, _p, _i, _p, _d, ctypes.POINTER(HgbCosmo), _p, _p, _p, _p, _p, _p,
                              _p]),
     ("hgb_loudest_par_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
@@ -169,7 +170,7 @@ KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
-    "hgb_loudest_hc_from_sorted": 6, "hgb_sam_poisson_gwb": 2, "hgb_param_grids": 1, "hgb_model_details": 9,
+    "hgb_loudest_hc_from_sorted": 6, "hgb_loudest_hc_from_sorted_ex": 6, "hgb_sam_poisson_gwb": 2, "hgb_param_grids": 1, "hgb_model_details": 9,
     "hgb_loudest_hc_and_par_from_sorted": 6,
 }
 _launches = [0]

@@ -160,7 +160,9 @@ __constant__ float c_invf[NT] = {
 // small-lambda pass finishes before the first table is built.
 struct Tile {
     union {
-        unsigned int thr[NT][RB];                 // small lambda: floor(CDF(n) 2^32), n = 0..31
+        // small lambda: floor(CDF(n) 2^32), n = 0..31, one padded row per bin: the lanes of a warp
+        // search one bin's row at different n, which the padding puts in different banks
+        unsigned int thr[RB][NT + 1];
         unsigned int arena[ARENA_WORDS];          // table kind: packed cdf (u32) + guide (u16) tables
     } u;
     unsigned long long tskip[RB];     // tiny lambda: floor(e^(-RPT lambda) 2^64): no hit in RPT draws
@@ -216,13 +218,13 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
         for (; n < NT - 1; n++) {
             if (n > 0) p = p * lf * c_invf[n];
             cum += __float2uint_rn(p * 0x1.0p32f);
-            s.u.thr[n][j] = (cum < 0xFFFFFFFFull) ? (unsigned int)cum : 0xFFFFFFFFu;
+            s.u.thr[j][n] = (cum < 0xFFFFFFFFull) ? (unsigned int)cum : 0xFFFFFFFFu;
             if ((float)n > lf && p < 0x1.0p-34f) {
                 n++;
                 break;
             }
         }
-        for (; n < NT; n++) s.u.thr[n][j] = 0xFFFFFFFFu;
+        for (; n < NT; n++) s.u.thr[j][n] = 0xFFFFFFFFu;
     } else if (kind == KIND_TABLE || kind == KIND_PTRS32) {
         const float lf = (float)lam;
         const double li = floor(lam);
@@ -535,6 +537,7 @@ int cumulate(long nb, int nf, const double *lam_s, const double *h_mask, double 
 struct PrefixArgs {
     long nb;
     int nf, nr, nl;
+    int f_offset;     // global index of the first frequency (counters use global frequencies)
     PhiloxKey key;
 };
 
@@ -582,7 +585,8 @@ __global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict
             hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
             break;
         }
-        const uint4 ctr = make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX);
+        const uint32_t fg = (uint32_t)(f + a.f_offset);
+        const uint4 ctr = make_uint4((uint32_t)r, fg, e, W_PREFIX);
         const uint4 w = philox(ctr, a.key);
         const double target = C[i] - log1p(-u53(w.x, w.y));   // C[i] + Exp(1)
         if (!(total > target)) {   // no further source in this realization
@@ -599,13 +603,13 @@ __global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict
         const double lj = lam[j];
         double num;
         if (lj > NORMAL_THRESH) {
-            num = normal_draw(make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX | 0x8000u), a.key, lj);
+            num = normal_draw(make_uint4((uint32_t)r, fg, e, W_PREFIX | 0x8000u), a.key, lj);
         } else if (lj < PTRS_MIN) {
             num = (double)truncated_count(lj, u53(w.z, w.w), d_status);
         } else {
             num = 0.0;
             for (int rep = 0; rep < 64 && num < 1.0; rep++)
-                num = ptrs64(make_uint4((uint32_t)r, (uint32_t)f, e, W_PREFIX | ((uint32_t)(rep + 1) << 8)), a.key,
+                num = ptrs64(make_uint4((uint32_t)r, fg, e, W_PREFIX | ((uint32_t)(rep + 1) << 8)), a.key,
                              lj, d_status);
             if (num < 1.0) {
                 hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
@@ -652,6 +656,7 @@ __global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict
 struct BulkArgs {
     long nb;
     int nf, nr;
+    int f_offset;      // global index of the first frequency (counters use global frequencies)
     int nchunk;        // chunk c holds tiles c, c + nchunk, c + 2 nchunk, ...
     uint32_t domain;
     PhiloxKey key;
@@ -816,7 +821,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
     __syncthreads();
     const int block_qmin = SORTED ? q_min_s : 0;
     const int block_qmax = SORTED ? q_max_s : 0;
-    const uint4 ctr0 = make_uint4(0u, (uint32_t)r0, (uint32_t)f, a.domain);
+    const uint4 ctr0 = make_uint4(0u, (uint32_t)r0, (uint32_t)(f + a.f_offset), a.domain);
     // first bulk position of slot sl, for the passes whose slot is data dependent
     const int *q_row = SORTED ? qpos + (long)f * a.nr + r0 : nullptr;
     const long ntiles = (a.nb + RB - 1) / RB;
@@ -872,7 +877,8 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
             const int j = s.list[KIND_SMALL][li];
             const int pos = s.pos[j];
             const float hs = s.hs[j];
-            const unsigned int t0 = s.u.thr[0][j];
+            const unsigned int *row = s.u.thr[j];
+            const unsigned int t0 = row[0];
 #pragma unroll
             for (int call = 0; call < RPT / 4; call++) {
                 if (4 * call >= rpt) break;
@@ -886,12 +892,12 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                     const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
                     if (sl >= rpt || u < t0) continue;
                     int n = 0;
-                    if (u >= s.u.thr[n + 15][j]) n += 16;
-                    if (u >= s.u.thr[n + 7][j]) n += 8;
-                    if (u >= s.u.thr[n + 3][j]) n += 4;
-                    if (u >= s.u.thr[n + 1][j]) n += 2;
-                    if (u >= s.u.thr[n][j]) n += 1;
-                    if (n == NT - 1 && u >= s.u.thr[NT - 1][j]) n = small_tail(s.lam[j], u, d_status);
+                    if (u >= row[n + 15]) n += 16;
+                    if (u >= row[n + 7]) n += 8;
+                    if (u >= row[n + 3]) n += 4;
+                    if (u >= row[n + 1]) n += 2;
+                    if (u >= row[n]) n += 1;
+                    if (n == NT - 1 && u >= row[NT - 1]) n = small_tail(s.lam[j], u, d_status);
                     if (!check || pos >= __ldg(q_row + sl * RB)) {
                         kahan_add(acc_r[sl], comp_r[sl], (float)n * hs);
                         if (PARAMS) add_par(psm, sl, t, j, (float)n);
@@ -1277,11 +1283,12 @@ LoudLayout loud_layout(long nb, int nf, int nr, int mode) {
     return L;
 }
 
-BulkArgs bulk_args(long nb, int nf, int nr, int nchunk, uint64_t seed, uint32_t domain) {
+BulkArgs bulk_args(long nb, int nf, int nr, int nchunk, uint64_t seed, uint32_t domain, int f_offset = 0) {
     BulkArgs a;
     a.nb = nb;
     a.nf = nf;
     a.nr = nr;
+    a.f_offset = f_offset;
     a.nchunk = nchunk;
     a.domain = domain;
     a.key = make_key(seed);
@@ -1340,6 +1347,15 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
                                int nloud, const int32_t *order, int mode, uint64_t seed, const double *replay,
                                double *hc2ss, double *hc2bg, void *workspace, size_t workspace_bytes,
                                int *d_status, void *stream) {
+    return hgb_loudest_hc_from_sorted_ex(number, h2fdf, n_bins, n_freq, nreals, nloud, order, mode, seed, replay,
+                                         hc2ss, hc2bg, workspace, workspace_bytes, d_status, stream, 0);
+}
+
+int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, long n_bins, int n_freq, int nreals,
+                                  int nloud, const int32_t *order, int mode, uint64_t seed, const double *replay,
+                                  double *hc2ss, double *hc2bg, void *workspace, size_t workspace_bytes,
+                                  int *d_status, void *stream, int freq_offset) {
+    HGB_CHECK_ARG(freq_offset >= 0 && (long)freq_offset + n_freq <= 65535);
     HGB_CHECK_ARG(number && h2fdf && order && hc2bg && n_bins >= 0 && n_freq >= 1 && nreals >= 0 && nloud >= 0);
     HGB_CHECK_ARG(nloud == 0 || hc2ss);
     HGB_CHECK_ARG(nloud <= 255);
@@ -1378,11 +1394,12 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
     pa.nf = n_freq;
     pa.nr = nreals;
     pa.nl = nloud;
+    pa.f_offset = freq_offset;
     pa.key = make_key(seed);
     k_loud_prefix<false><<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(pa, ParArgs{}, lam_s, h_s, cum, hc2ss, bgp,
                                                                             q, d_status);
     if ((rc = hgb::check_launch())) return rc;
-    BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u);
+    BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u, freq_offset);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
     if ((rc = bulk_event(0, st))) return rc;
     k_bulk<true, false><<<grid, RB, 0, st>>>(a, ParArgs{}, lam_s, h_s, q, part, d_status);
@@ -1464,6 +1481,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     pf.nf = n_freq;
     pf.nr = nreals;
     pf.nl = nloud;
+    pf.f_offset = 0;
     pf.key = make_key(seed);
     k_loud_prefix<true><<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(pf, pa, lam_s, h_s, cum, hc2ss, bgp, q,
                                                                            d_status);

@@ -30,14 +30,28 @@ def _check_threshold(normal_threshold):
         raise ValueError(f"normal_threshold={normal_threshold}: only the reference default 1e10 is supported")
 
 
-def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=None, status=None):
-    """Device (hc2ss[F, R, L], hc2bg[F, R]) from device number/h2fdf (B, F) and order (B,) int32."""
+def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=None, status=None, freq_offset=0,
+                   out=None):
+    """Device (hc2ss[F, R, L], hc2bg[F, R]) from device number/h2fdf (B, F) and order (B,) int32.
+
+    ``freq_offset``: the global index of column 0 in a frequency chunk of a wider run; Philox draws
+    are keyed by the global frequency, so chunk results equal the same frequencies' results of one
+    call over the whole band.  ``out``: preallocated contiguous (hc2ss, hc2bg) to write into.
+    """
     t = D.torch()
     nf = int(number.shape[-1])
     nb = int(number.numel() // nf)
     dev = number.device
-    hc2ss = t.empty((nf, nreals, nloudest), dtype=t.float64, device=dev)
-    hc2bg = t.empty((nf, nreals), dtype=t.float64, device=dev)
+    if out is None:
+        hc2ss = t.empty((nf, nreals, nloudest), dtype=t.float64, device=dev)
+        hc2bg = t.empty((nf, nreals), dtype=t.float64, device=dev)
+    else:
+        hc2ss, hc2bg = out
+        if (tuple(hc2ss.shape) != (nf, nreals, nloudest) or tuple(hc2bg.shape) != (nf, nreals)
+                or not (hc2ss.is_contiguous() and hc2bg.is_contiguous())):
+            raise ValueError("out must be contiguous (F, R, L) and (F, R) float64 tensors")
+    if freq_offset and replay is not None:
+        raise ValueError("freq_offset applies to Philox draws only")
     mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
     rep = None
     if replay is not None:
@@ -49,9 +63,9 @@ def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=Non
     ws = D.workspace(ws_bytes, dev)
     st = status if status is not None else D.StatusWord(dev)
     seed = new_seed() if seed is None else int(seed) & 0xFFFFFFFFFFFFFFFF
-    N.call("hgb_loudest_hc_from_sorted", N.ptr(number), N.ptr(h2fdf), nb, nf, int(nreals), int(nloudest),
+    N.call("hgb_loudest_hc_from_sorted_ex", N.ptr(number), N.ptr(h2fdf), nb, nf, int(nreals), int(nloudest),
            N.ptr(order), mode, seed, N.ptr(rep), N.ptr(hc2ss), N.ptr(hc2bg), N.ptr(ws), int(ws_bytes), st.ptr,
-           N.stream_handle())
+           N.stream_handle(), int(freq_offset))
     return hc2ss, hc2bg
 
 

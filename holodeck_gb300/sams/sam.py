@@ -211,7 +211,9 @@ class Semi_Analytic_Model:
         return single_sources.ss_realize_device(number, h2fdf, realize, loudest, seed=seed, replay=replay,
                                                 order=order)
 
-    def _number_and_strain(self, fobs_orb_edges, diff_num, redz_final):
+    def _number_and_strain(self, fobs_orb_edges, diff_num, redz_final, status=None):
+        """Device (number, h2fdf) on the (M-1, Q-1, Z-1, F) bins.  With ``status`` the redshift check
+        is left to the caller (no host read here)."""
         t = D.torch()
         mt, mr, rz = self._edges_device()
         lm = D.as_device(np.log10(self.mtot))
@@ -222,11 +224,12 @@ class Semi_Analytic_Model:
         nf = int(dlnf.numel())
         number = t.empty((nm - 1, nq - 1, nz - 1, nf), dtype=t.float64, device=mt.device)
         h2fdf = t.empty_like(number)
-        st = D.StatusWord(mt.device)
+        st = D.StatusWord(mt.device) if status is None else status
         N.call("hgb_number_and_strain", N.ptr(mt), N.ptr(lm), nm, N.ptr(mr), nq, N.ptr(rz), nz, N.ptr(fe),
                N.ptr(dlnf), nf, N.ptr(diff_num), N.ptr(redz_final), C.GW_SRC_CONST, dc.ref, N.ptr(number),
                N.ptr(h2fdf), st.ptr, N.stream_handle())
-        single_sources.check_redshift_status(st)
+        if status is None:
+            single_sources.check_redshift_status(st)
         return number, h2fdf
 
     def gwb(self, fobs_gw_edges, hard=None, realize=100, loudest=1, params=False, seed=None, replay=None,

@@ -50,7 +50,11 @@ def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None
     dc = D.device_cosmology(cosmo)
     fo = D.as_device(fobs_orb)
     nf = int(fo.numel())
-    sorted_ok = int(bool(t.all(fo[1:] >= fo[:-1]).item())) if nf > 1 else 1
+    if D.is_torch(fobs_orb):
+        sorted_ok = int(bool(t.all(fo[1:] >= fo[:-1]).item())) if nf > 1 else 1
+    else:   # host input: decide on the host, no device round trip
+        fh = np.asarray(fobs_orb, dtype=np.float64).ravel()
+        sorted_ok = int(bool(np.all(fh[1:] >= fh[:-1])))
     shape = tuple(dens.shape) + (nf,)
     redz_final = t.empty(shape, dtype=t.float64, device=dens.device)
     diff_num = t.empty(shape, dtype=t.float64, device=dens.device)

@@ -266,6 +266,15 @@ int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n
                                const double *replay, double *hc2ss, double *hc2bg,
                                void *workspace, size_t workspace_bytes, int *d_status, void *stream);
 
+/* hgb_loudest_hc_from_sorted on a run of frequencies that starts at global frequency index
+ * freq_offset: number / h2fdf / hc2ss / hc2bg hold only the n_freq frequencies of the run, and the
+ * Philox counters use the global index, so splitting the frequencies over several calls gives the
+ * same draws as one call (order is still the loudest-first order of the first global frequency). */
+int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, long n_bins, int n_freq, int nreals,
+                                  int nloud, const int32_t *order, int mode, uint64_t seed, const double *replay,
+                                  double *hc2ss, double *hc2bg, void *workspace, size_t workspace_bytes,
+                                  int *d_status, void *stream, int freq_offset);
+
 /* Parameter grids of ss_gws_redz(params=True) (single_sources.py:117-143) on the (B, F) bins:
  * redz_mid = the redshift midpoints of redz_final along mtot, mrat, redz (-1 where <= 0),
  * dcom = comoving distance of redz_mid (+inf where it is -1), sepa = Kepler separation
