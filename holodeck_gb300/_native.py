@@ -170,7 +170,7 @@ KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
-    "hgb_loudest_hc_from_sorted": 6, "hgb_loudest_hc_from_sorted_ex": 6, "hgb_sam_poisson_gwb": 2, "hgb_param_grids": 1, "hgb_model_details": 9,
+    "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
     "hgb_loudest_hc_and_par_from_sorted": 6,
 }
 _launches = [0]

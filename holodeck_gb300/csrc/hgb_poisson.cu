@@ -33,21 +33,25 @@
 // the 64-bit seed; counters are built from (sorted bin or event index, realization, frequency,
 // draw family), so results do not depend on the chunking.  Bulk samplers by expectation lambda:
 //   lambda <= 0 or NaN        n = 0, no draw
-//   lambda < TINY             geometric skipping over a lane's realizations: the gap to the next
-//                             realization with n >= 1 is floor(-ln u / lambda), so one 64-bit
-//                             uniform usually settles all RPT realizations; a hit draws n from the
-//                             zero-truncated Poisson
-//   TINY <= lambda < 10       inversion of a 32-bit uniform against the bin's table of
+//   lambda < SPARSE_MAX       geometric skipping over realizations: the gap to the next realization
+//                             with n >= 1 is floor(-ln u / lambda), and a hit draws n from the
+//                             zero-truncated Poisson.  The block's realizations are cut into runs of
+//                             2^lg (about one expected event each) and one thread walks a run, so a
+//                             bin costs about one draw per event instead of one per lane
+//   SPARSE_MAX <= lambda < 10 inversion of a 32-bit uniform against the bin's table of
 //                             floor(CDF(n) 2^32), n < 32, by a branch-free binary search; four
 //                             realizations per Philox call
-//   10 <= lambda < 2^22       PTRS, transformed rejection with squeeze (Hormann 1993, Insurance:
+//   10 <= lambda <= 65536     inversion against a per-bin table over lambda +- 7 sqrt(lambda) in
+//                             shared memory, with a guide table whose "pure" cells answer most draws
+//                             with one lookup; four realizations per Philox call
+//   65536 < lambda < 2^22     PTRS, transformed rejection with squeeze (Hormann 1993, Insurance:
 //                             Mathematics and Economics 12, 39-45) in FP32: the acceptance test uses
 //                             the log-pmf in Loader's saddle-point form (bd0 + Stirling remainder,
 //                             Loader 2000), so nothing cancels in FP32.  Each lane runs one loop
 //                             over its realizations that consumes two attempts per Philox call and
 //                             moves to the next realization on acceptance, so a rejection delays
 //                             only its own lane by one attempt
-//   2^22 <= lambda <= 1e10    PTRS in FP64
+//   2^22 <= lambda <= 1e10    PTRS in FP64 (k_bulk_wide, after k_bulk)
 //   lambda > 1e10             Normal(lambda, sqrt(lambda)) by Box-Muller, as the reference does
 // Counts are integers; background sums accumulate n * h2fdf * 2^100 in FP32 with Kahan
 // compensation (relative error ~1e-7 of hc^2); the loudest slots hold the exact float64 h2fdf.
@@ -68,7 +72,7 @@ constexpr int NWARP = RB / 32;
 constexpr int RPT = 8;                   // realizations per thread
 static_assert(RPT % 4 == 0, "the table passes draw four realizations per Philox call");
 constexpr int NT = 32;                   // CDF thresholds per small-lambda bin
-constexpr double TINY = 0.02;            // geometric skipping below this expectation
+constexpr double SPARSE_MAX = 0.1;       // geometric skipping over realizations below this expectation
 constexpr double NORMAL_THRESH = 1e10;   // long(1e10) in cyutils.pyx:1223
 constexpr double PTRS_MIN = 10.0;
 constexpr double PTRS32_MAX = 4194304.0; // 2^22: k stays exact in FP32
@@ -88,6 +92,7 @@ constexpr uint32_t W_SMALL = 0x00000000u;   // | call: 4 realizations per call
 constexpr uint32_t W_PTRS = 0x10000000u;    // | iteration / 2
 constexpr uint32_t W_TABLE = 0x50000000u;   // | call: 4 realizations per call
 constexpr uint32_t W_SKIP = 0x20000000u;    // | step: geometric skipping of a lane's realizations
+constexpr uint32_t W_SPARSE = 0x60000000u;  // | event: geometric skipping along a run of realizations
 constexpr uint32_t W_WIDE = 0x30000000u;    // | slot << 8 | attempt: PTRS64 / Normal draws
 constexpr uint32_t W_PREFIX = 0x40000000u;  // | attempt: prefix events (counter .z = event index)
 constexpr uint32_t DOMAIN_GWB = 0x80000000u;
@@ -95,7 +100,7 @@ constexpr float HSCALE = 0x1.0p100f;     // keeps h2fdf (1e-30 .. 1e-20) far fro
 constexpr double HSCALE_INV = 0x1.0p-100;
 
 enum BinKind : int {
-    KIND_NONE = 0, KIND_TINY = 1, KIND_SMALL = 2, KIND_TABLE = 3, KIND_PTRS32 = 4, KIND_WIDE = 5, NKIND = 6
+    KIND_NONE = 0, KIND_SPARSE = 1, KIND_SMALL = 2, KIND_TABLE = 3, KIND_PTRS32 = 4, KIND_WIDE = 5, NKIND = 6
 };
 
 // ---- Philox4x32-10 with the ten round keys precomputed (they live in the kernel's parameter space)
@@ -165,7 +170,8 @@ struct Tile {
         unsigned int thr[RB][NT + 1];
         unsigned int arena[ARENA_WORDS];          // table kind: packed cdf (u32) + guide (u16) tables
     } u;
-    unsigned long long tskip[RB];     // tiny lambda: floor(e^(-RPT lambda) 2^64): no hit in RPT draws
+    unsigned char sp_lg[RB];          // sparse: log2 of the realization run length of the bin
+    int sp_start[RB];                 // sparse: first run of each sparse-list entry
     unsigned long long scan[NWARP];
     double lam[RB];
     float hs[RB];                     // h2fdf * 2^100 (for the background sums)
@@ -194,7 +200,7 @@ struct Slots {
 
 __device__ __forceinline__ int bin_kind(double lam) {
     if (!(lam > 0.0)) return KIND_NONE;
-    if (lam < TINY) return KIND_TINY;
+    if (lam < SPARSE_MAX) return KIND_SPARSE;
     if (lam < PTRS_MIN) return KIND_SMALL;
     if (lam <= TABLE_MAX) return KIND_TABLE;
     if (lam < PTRS32_MAX) return KIND_PTRS32;
@@ -204,10 +210,11 @@ __device__ __forceinline__ int bin_kind(double lam) {
 __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
     s.lam[j] = lam;
     s.hs[j] = (float)(h * (double)HSCALE);
-    if (kind == KIND_TINY) {
-        // u < tskip <=> no source in RPT draws; 1 - e^(-RPT lambda) to FP32 relative precision
-        const float miss = -expm1f(-(float)RPT * (float)lam);
-        s.tskip[j] = ~__float2ull_rn(miss * 0x1.0p64f);
+    if (kind == KIND_SPARSE) {
+        // runs of 2^lg realizations, lambda 2^lg in [0.5, 1) unless clamped to [8, 1024]
+        const float lf = (float)lam;
+        s.lamf[j] = lf;
+        s.sp_lg[j] = (unsigned char)(lf > 0.0f ? max(3, min(10, -ilogbf(lf) - 1)) : 10);
     } else if (kind == KIND_SMALL) {
         // P(n) in FP32 by the recursion P(n) = P(n-1) lambda / n, rounded to 32.32 fixed point and
         // summed exactly; the last threshold is saturated (P(n >= 31) < 1e-8 for lambda < 10)
@@ -359,7 +366,7 @@ __device__ int truncated_count(double lam, double v, int *d_status) {
     return n;
 }
 
-// Zero-truncated Poisson for lambda < TINY in FP32 (P(n >= 2) ~ lambda / 2).
+// Zero-truncated Poisson for lambda < SPARSE_MAX in FP32 (P(n >= 2) ~ lambda / 2).
 __device__ int truncated_count_f32(float lam, float v, int *d_status) {
     float p = lam / expm1f(lam);      // P(n = 1 | n >= 1)
     float cdf = p;
@@ -662,69 +669,112 @@ struct BulkArgs {
     PhiloxKey key;
 };
 
-// Builds the inversion table of one table-kind bin (lambda in [10, TABLE_MAX]) with one warp:
-// P(k) for k = k_lo .. k_lo + S - 1 in FP32 (the Loader form at every ANCHOR-th entry, the recursion
-// P(k) = P(k-1) lambda / k in between), rounded to 32.32 fixed point, summed exactly in integers
-// (warp scan) into cdf[m] = floor(CDF 2^32), and 2^gb >= S guide cells:
-// guide[i] = smallest m with cdf[m] > i 2^(32 - gb).  The mass outside the range (< 1e-11) goes to
-// the end entries.
+// Inversion table of one table-kind bin (lambda in [10, TABLE_MAX]), built by a warp or a block:
+//   cdf[m]   = min(sum of q(k_lo) .. q(k_lo + m), 2^32 - 1), with q(k) = P(k) in 32.32 fixed point
+//              (rounded to nearest); cdf[S - 1] = 2^32 - 1, so the mass outside the range (< 1e-11)
+//              goes to the end entries;
+//   guide[c] = smallest m with cdf[m] > c 2^(32 - gb), for the 2^gb >= S cells, with bit 15 set when
+//              cdf[m] >= (c + 1) 2^(32 - gb): every u in the cell then maps to m ("pure" cell).
+// P(k) is FP32: the Loader form at every ANCHOR-th entry and the recursion P(k) = P(k-1) lambda / k
+// in between (__fdividef: at most 2 ulp per step, so under 16 ulp of drift before the next anchor).
+// Each thread takes E consecutive entries; the guide is the merge of the cdf values with the cell
+// starts, split evenly over the threads (merge path), so no thread waits on another's long run of
+// cells or entries.
+
+// q of the entries m0 .. m1 - 1 into cdf[m]; returns their sum, which stays below 2^31 (a thread's
+// entries span at most 1/32 of the table, well under half the probability)
+__device__ __forceinline__ unsigned table_pmf(const Tile &s, int j, unsigned int *cdf, int m0, int m1) {
+    const int k_lo = s.tb_klo[j], lam_int = s.lam_int[j];
+    const float frac = s.frac[j], lamf = s.lamf[j];
+    unsigned local = 0;
+    for (int a = m0; a < m1; a += ANCHOR) {
+        float kf = (float)(k_lo + a);   // exact: k < 2^24
+        float p = pmf_f32(k_lo + a, lam_int, frac, lamf);
+        unsigned q = __float2uint_rn(p * 0x1.0p32f);
+        cdf[a] = q;
+        local += q;
+        const int n = min(ANCHOR, m1 - a);
+#pragma unroll
+        for (int i = 1; i < ANCHOR; i++) {
+            if (i < n) {
+                kf += 1.0f;
+                p *= __fdividef(lamf, kf);
+                q = __float2uint_rn(p * 0x1.0p32f);
+                cdf[a + i] = q;
+                local += q;
+            }
+        }
+    }
+    return local;
+}
+
+// running sums of the thread's entries on top of base (the 64-bit sum of every earlier entry),
+// saturated at 2^32 - 1 with 32-bit arithmetic
+__device__ __forceinline__ void table_prefix(unsigned int *cdf, int m0, int m1, unsigned long long base) {
+    const bool full = base >= 0xFFFFFFFFull;
+    const unsigned b32 = full ? 0xFFFFFFFFu : (unsigned)base;
+    const unsigned room = full ? 0u : (unsigned)(0xFFFFFFFFull - base);
+    unsigned run = 0;
+    for (int m = m0; m < m1; m++) {
+        run += cdf[m];
+        cdf[m] = b32 + min(run, room);
+    }
+}
+
+// the guide cells from the finished cdf: thread t of nthr walks diagonals [d0, d1) of the merge of
+// cdf[0 .. S-1] with the cell starts c 2^shift (a cdf value goes first on ties)
+__device__ __forceinline__ void table_guide(const unsigned int *cdf, unsigned short *guide, int S, int gb, int t,
+                                            int nthr) {
+    const int shift = 32 - gb, nc = 1 << gb;
+    const int total = S + nc;
+    const int D = (total + nthr - 1) / nthr;
+    const int d0 = min(t * D, total), d1 = min(d0 + D, total);
+    int lo = max(0, d0 - nc), hi = min(d0, S);   // cdf values among the first d0 merged elements
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] <= ((unsigned)(d0 - 1 - mid) << shift)) lo = mid + 1;
+        else hi = mid;
+    }
+    int m = lo, c = d0 - lo;
+    unsigned am = cdf[min(m, S - 1)];
+    for (int d = d0; d < d1 && c < nc; d++) {
+        if (am <= ((unsigned)c << shift)) {   // m < S - 1: cdf[S - 1] = 2^32 - 1 exceeds every cell start
+            m++;
+            am = cdf[m];
+        } else {
+            guide[c] = (unsigned short)(m | ((am >> shift) > (unsigned)c ? 0x8000 : 0));
+            c++;
+        }
+    }
+}
+
+// one warp builds the table of bin j (tables of at most HALF_WORDS words)
 __device__ void build_table_warp(const Tile &s, int j, unsigned int *cdf, unsigned short *guide, int lane) {
-    const int S = s.tb_S[j], k_lo = s.tb_klo[j], shift = 32 - s.tb_gb[j];
+    const int S = s.tb_S[j];
     const int E = (S + 31) >> 5;
     const int m0 = min(lane * E, S), m1 = min(m0 + E, S);
-    const int lam_int = s.lam_int[j];
-    const float frac = s.frac[j], lamf = s.lamf[j];
-    unsigned long long local = 0;
-    float p = 0.0f;
-    for (int m = m0; m < m1; m++) {
-        const int k = k_lo + m;
-        if (((m - m0) & (ANCHOR - 1)) == 0) p = pmf_f32(k, lam_int, frac, lamf);
-        else p = p * lamf / (float)k;   // correctly rounded steps: < 4 ulp drift before the next anchor
-        const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
-        cdf[m] = qm;
-        local += qm;
-    }
+    const unsigned local = table_pmf(s, j, cdf, m0, m1);
     unsigned long long incl = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += y;
     }
-    unsigned long long run = incl - local;
-    const unsigned long long cell = 1ull << shift;
-    const unsigned int ncell = 1u << (32 - shift);
-    unsigned long long prev = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;   // cdf[m0 - 1]
-    for (int m = m0; m < m1; m++) {
-        run += cdf[m];
-        const unsigned long long cur = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
-        cdf[m] = (unsigned int)cur;
-        const unsigned int lo = (m == 0) ? 0u : (unsigned int)((prev + cell - 1) >> shift);
-        const unsigned int hi = (m == S - 1) ? ncell : (unsigned int)((cur + cell - 1) >> shift);
-        for (unsigned int i = lo; i < hi; i++) guide[i] = (unsigned short)m;
-        prev = cur;
-    }
+    table_prefix(cdf, m0, m1, incl - local);
+    if (m0 < S && m1 == S) cdf[S - 1] = 0xFFFFFFFFu;
+    __syncwarp();
+    table_guide(cdf, guide, S, s.tb_gb[j], lane, 32);
     __syncwarp();
 }
 
-// The same table built by the whole block (for large tables): entries spread over all threads, the
-// integer prefix sums by a block scan.  Starts and ends with a barrier-protected table.
+// the whole block builds the table of bin j (large tables); starts and ends with a barrier-protected
+// table
 __device__ void build_table_block(Tile &s, int j, unsigned int *cdf, unsigned short *guide) {
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int S = s.tb_S[j], k_lo = s.tb_klo[j], shift = 32 - s.tb_gb[j];
+    const int S = s.tb_S[j];
     const int E = (S + RB - 1) / RB;
     const int m0 = min(t * E, S), m1 = min(m0 + E, S);
-    const int lam_int = s.lam_int[j];
-    const float frac = s.frac[j], lamf = s.lamf[j];
-    unsigned long long local = 0;
-    float p = 0.0f;
-    for (int m = m0; m < m1; m++) {
-        const int k = k_lo + m;
-        if (((m - m0) & (ANCHOR - 1)) == 0) p = pmf_f32(k, lam_int, frac, lamf);
-        else p = p * lamf / (float)k;
-        const unsigned int qm = __float2uint_rn(p * 0x1.0p32f);
-        cdf[m] = qm;
-        local += qm;
-    }
+    const unsigned local = table_pmf(s, j, cdf, m0, m1);
     unsigned long long incl = local;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -733,20 +783,12 @@ __device__ void build_table_block(Tile &s, int j, unsigned int *cdf, unsigned sh
     }
     if (lane == 31) s.scan[warp] = incl;
     __syncthreads();
-    unsigned long long run = incl - local;
-    for (int w = 0; w < warp; w++) run += s.scan[w];
-    const unsigned long long cell = 1ull << shift;
-    const unsigned int ncell = 1u << (32 - shift);
-    unsigned long long prev = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
-    for (int m = m0; m < m1; m++) {
-        run += cdf[m];
-        const unsigned long long cur = (run < 0xFFFFFFFFull) ? run : 0xFFFFFFFFull;
-        cdf[m] = (unsigned int)cur;
-        const unsigned int lo = (m == 0) ? 0u : (unsigned int)((prev + cell - 1) >> shift);
-        const unsigned int hi = (m == S - 1) ? ncell : (unsigned int)((cur + cell - 1) >> shift);
-        for (unsigned int i = lo; i < hi; i++) guide[i] = (unsigned short)m;
-        prev = cur;
-    }
+    unsigned long long base = incl - local;
+    for (int w = 0; w < warp; w++) base += s.scan[w];
+    table_prefix(cdf, m0, m1, base);
+    if (m0 < S && m1 == S) cdf[S - 1] = 0xFFFFFFFFu;
+    __syncthreads();
+    table_guide(cdf, guide, S, s.tb_gb[j], t, RB);
     __syncthreads();
 }
 
@@ -879,13 +921,18 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
             const float hs = s.hs[j];
             const unsigned int *row = s.u.thr[j];
             const unsigned int t0 = row[0];
+            uint4 wv[RPT / 4];   // every call issued first: independent round chains interleave
 #pragma unroll
             for (int call = 0; call < RPT / 4; call++) {
-                if (4 * call >= rpt) break;
                 uint4 ctr = ctr0;
                 ctr.x = (uint32_t)pos;
                 ctr.w |= W_SMALL | (uint32_t)call;
-                const uint4 w = philox(ctr, a.key);
+                wv[call] = philox(ctr, a.key);
+            }
+#pragma unroll
+            for (int call = 0; call < RPT / 4; call++) {
+                if (4 * call >= rpt) break;
+                const uint4 w = wv[call];
 #pragma unroll
                 for (int m = 0; m < 4; m++) {
                     const int sl = 4 * call + m;
@@ -979,20 +1026,28 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                     const unsigned int *cdf = s.u.arena + off;
                     const unsigned short *guide = (const unsigned short *)(s.u.arena + off + S);
                     off += table_words(s, j);
+                    uint4 wv[RPT / 4];   // every call issued first: independent round chains interleave
 #pragma unroll
                     for (int call = 0; call < RPT / 4; call++) {
-                        if (4 * call >= rpt) break;
                         uint4 ctr = ctr0;
                         ctr.x = (uint32_t)pos;
                         ctr.w |= W_TABLE | (uint32_t)call;
-                        const uint4 w = philox(ctr, a.key);
+                        wv[call] = philox(ctr, a.key);
+                    }
+#pragma unroll
+                    for (int call = 0; call < RPT / 4; call++) {
+                        if (4 * call >= rpt) break;
+                        const uint4 w = wv[call];
 #pragma unroll
                         for (int m = 0; m < 4; m++) {
                             const int sl = 4 * call + m;
                             const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
                             if (sl >= rpt) continue;
-                            int e = guide[u >> shift];
-                            while (e < S - 1 && u >= cdf[e]) e++;
+                            const uint32_t uc = min(u, 0xFFFFFFFEu);   // below cdf[S - 1]
+                            const unsigned g = guide[uc >> shift];
+                            int e = (int)(g & 0x7FFFu);
+                            if (!(g & 0x8000u))
+                                while (uc >= cdf[e]) e++;
                             if (!check || pos >= __ldg(q_row + sl * RB)) {
                                 kahan_add(acc_r[sl], comp_r[sl], (float)(k_lo + e) * hs);
                                 if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + e));
@@ -1063,44 +1118,114 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
             }
         }
 
-        // ---- tiny lambda: geometric skipping over the lane's realizations
-        const int n_tiny = kind_count(s, KIND_TINY);
+        // ---- sparse (lambda < SPARSE_MAX): geometric skipping, the gap to the next realization with
+        // n >= 1 being floor(-ln u / lambda) and n zero-truncated Poisson
+        const int n_sparse = kind_count(s, KIND_SPARSE);
+        if (PARAMS) {
+            // the lane's own realizations, so the parameter sums stay thread-private
 #pragma unroll 1
-        for (int li = 0; li < n_tiny; li++) {
-            if (rpt == 0) break;
-            const int j = s.list[KIND_TINY][li];
-            const int pos = s.pos[j];
-            uint4 ctr = ctr0;
-            ctr.x = (uint32_t)pos;
-            ctr.w |= W_SKIP;
-            uint4 w = philox(ctr, a.key);
-            if (rpt == RPT && w64(w.x, w.y) < s.tskip[j]) continue;
-            const float lf = (float)s.lam[j];
-            const float hs = s.hs[j];
-            int i = 0;
-            for (int step = 0; step < 2 * RPT + 2; step++) {
-                if (step > 0) {
+            for (int li = 0; li < n_sparse; li++) {
+                if (rpt == 0) break;
+                const int j = s.list[KIND_SPARSE][li];
+                const int pos = s.pos[j];
+                const float lf = s.lamf[j];
+                const float hs = s.hs[j];
+                uint4 ctr = ctr0;
+                ctr.x = (uint32_t)pos;
+                ctr.w |= W_SKIP;
+                int i = 0;
+                for (int step = 0; step < 2 * RPT + 2; step++) {
                     uint4 cc = ctr;
                     cc.w |= (uint32_t)step;
-                    w = philox(cc, a.key);
+                    const uint4 w = philox(cc, a.key);
+                    // U = (u + 1) 2^-64 in (0, 1]: -ln U = -log1p(-x) with x = (2^64 - 1 - u) 2^-64
+                    const float x = fminf(__ull2float_rn(~w64(w.x, w.y)) * 0x1.0p-64f, 0.99999994f);
+                    const float gap = floorf(-log1pf(-x) / lf);
+                    if (gap >= (float)(rpt - i)) break;
+                    i += (int)gap;
+                    const int n = truncated_count_f32(lf, u24(w.z), d_status);
+                    if (!check || pos >= __ldg(q_row + i * RB)) {
+                        add_bg(st, i, t, (float)n * hs);
+                        add_par(psm, i, t, j, (float)n);
+                    }
+                    i++;
+                    if (i >= rpt) break;
                 }
-                // U = (u + 1) 2^-64 in (0, 1]: -ln U = -log1p(-x) with x = (2^64 - 1 - u) 2^-64
-                const float x = fminf(__ull2float_rn(~w64(w.x, w.y)) * 0x1.0p-64f, 0.99999994f);
-                const float gap = floorf(-log1pf(-x) / lf);
-                if (gap >= (float)(rpt - i)) break;
-                i += (int)gap;
-                const int n = truncated_count_f32(lf, u24(w.z), d_status);
-                if (!check || pos >= __ldg(q_row + i * RB)) {
-                    add_bg(st, i, t, (float)n * hs);
-                    if (PARAMS) add_par(psm, i, t, j, (float)n);
-                }
-                i++;
-                if (i >= rpt) break;
             }
+        } else if (n_sparse > 0) {
+            // The block's realizations cut into runs of 2^lg per bin (about one expected event per
+            // run); the runs of the tile's sparse bins are numbered in list order and shared out
+            // over the threads, each walking its run by geometric gaps.  Events go to per-tile FP32
+            // sums by realization in the arena (atomics; a few events per realization and tile),
+            // which each thread then folds into its Kahan sums.
+            float *sub = reinterpret_cast<float *>(s.u.arena);   // [RPT * RB], realization r at sub[r]
+            const int nr_blk = min(RB * RPT, a.nr - (int)blockIdx.z * RB * RPT);
+            int runs = 0;
+            if (t < n_sparse) {
+                const int lg = s.sp_lg[s.list[KIND_SPARSE][t]];
+                runs = (nr_blk + (1 << lg) - 1) >> lg;
+            }
+            int incl = runs;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            __syncthreads();   // the arena and the scan words are free
+            if (lane == 31) s.scan[warp] = (unsigned long long)incl;
+#pragma unroll
+            for (int i = 0; i < RPT; i++) sub[i * RB + t] = 0.0f;
+            __syncthreads();
+            int before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < NWARP; w++) {
+                const int v = (int)s.scan[w];
+                before += (w < warp) ? v : 0;
+                total += v;
+            }
+            if (t < n_sparse) s.sp_start[t] = before + incl - runs;
+            __syncthreads();
+            const int *q_blk = SORTED ? q_row - t : nullptr;   // first bulk positions of the block's realizations
+#pragma unroll 1
+            for (int k = t; k < total; k += RB) {
+                int lo = 0, hi = n_sparse - 1;   // the last list entry whose runs start at or before k
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s.sp_start[mid] <= k) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int j = s.list[KIND_SPARSE][lo];
+                const int lg = s.sp_lg[j];
+                const int run = k - s.sp_start[lo];   // < 128: runs hold at least 8 realizations
+                const int re = min((run + 1) << lg, nr_blk);
+                const float lf = s.lamf[j], hs = s.hs[j];
+                const int pos = s.pos[j];
+                const uint4 ctr = make_uint4((uint32_t)pos, ((uint32_t)blockIdx.z << 7) | (uint32_t)run,
+                                             (uint32_t)(f + a.f_offset), a.domain | W_SPARSE);
+                int r = run << lg;   // the next gap counts from here
+                // every event advances r, so a run takes at most 2^lg + 1 steps
+                for (int ev = 0; ev <= (1 << lg); ev++) {
+                    uint4 cc = ctr;
+                    cc.w |= (uint32_t)ev;
+                    const uint4 w = philox(cc, a.key);
+                    const float x = fminf(__ull2float_rn(~w64(w.x, w.y)) * 0x1.0p-64f, 0.99999994f);
+                    const float gap = floorf(-log1pf(-x) / lf);
+                    if (gap >= (float)(re - r)) break;
+                    r += (int)gap;
+                    const int n = truncated_count_f32(lf, u24(w.z), d_status);
+                    if (!check || pos >= __ldg(q_blk + r)) atomicAdd(&sub[r], (float)n * hs);
+                    if (++r >= re) break;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < RPT; i++)
+                if (i < rpt) kahan_add(acc_r[i], comp_r[i], sub[i * RB + t]);
         }
 
-        // ---- PTRS64 / Normal (real-valued counts, cyutils.pyx:1327-1330 / :887-891)
-        const int n_wide = kind_count(s, KIND_WIDE);
+        // ---- PTRS64 / Normal (real-valued counts, cyutils.pyx:1327-1330 / :887-891); without the
+        // parameter sums these bins go to k_bulk_wide, which keeps their FP64 code out of this kernel
+        const int n_wide = PARAMS ? kind_count(s, KIND_WIDE) : 0;
 #pragma unroll 1
         for (int li = 0; li < n_wide; li++) {
             const int j = s.list[KIND_WIDE][li];
@@ -1134,6 +1259,78 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                     ldexp(((double)pacc[o] - (double)pcomp[o]) * HSCALE_INV, pa.scale_log2[k]);
             }
     }
+}
+
+// ---- 4b. bins above PTRS32_MAX (PTRS64 / Normal in FP64) when k_bulk leaves them out: the same
+// grid, chunks and realizations as k_bulk, run after it on the same stream; each block adds its
+// wide bins' sums (FP64, bin order) to the partials k_bulk wrote, and blocks without wide bins
+// write nothing.
+template <bool SORTED>
+__global__ void __launch_bounds__(RB) k_bulk_wide(BulkArgs a, const double *__restrict__ lam_in,
+                                                   const double *__restrict__ h_in, const int *__restrict__ qpos,
+                                                   double *__restrict__ part, int *d_status) {
+    __shared__ double w_lam[RB], w_h[RB];
+    __shared__ int w_pos[RB];
+    __shared__ int w_count[NWARP];
+    const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    const int r0 = blockIdx.z * RB * RPT + t;
+    int rpt = 0;
+    while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
+    const int *q_row = SORTED ? qpos + (long)f * a.nr + r0 : nullptr;
+    const uint4 ctr0 = make_uint4(0u, (uint32_t)r0, (uint32_t)(f + a.f_offset), a.domain);
+    double acc[RPT];
+#pragma unroll
+    for (int i = 0; i < RPT; i++) acc[i] = 0.0;
+    bool any = false;   // block-uniform
+    const long ntiles = (a.nb + RB - 1) / RB;
+    for (long tile = c; tile < ntiles; tile += a.nchunk) {
+        const long base = tile * RB;
+        const int nt = (int)((a.nb - base) < RB ? (a.nb - base) : RB);
+        bool wide = false;
+        double lam = 0.0;
+        if (t < nt) {
+            lam = SORTED ? lam_in[(long)f * a.nb + base + t] : lam_in[(base + t) * a.nf + f];
+            wide = bin_kind(lam) == KIND_WIDE;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, wide);
+        __syncthreads();   // the previous tile's list is drawn
+        if (lane == 0) w_count[warp] = __popc(m);
+        __syncthreads();
+        int off = 0, n = 0;
+#pragma unroll
+        for (int w = 0; w < NWARP; w++) {
+            off += (w < warp) ? w_count[w] : 0;
+            n += w_count[w];
+        }
+        if (wide) {
+            const int k = off + __popc(m & ((1u << lane) - 1u));
+            w_lam[k] = lam;
+            w_h[k] = SORTED ? h_in[(long)f * a.nb + base + t] : h_in[(base + t) * a.nf + f];
+            w_pos[k] = (int)(base + t);
+        }
+        if (n == 0) continue;
+        any = true;
+        __syncthreads();
+#pragma unroll 1
+        for (int li = 0; li < n; li++) {
+            const double lj = w_lam[li], hj = w_h[li];
+            const int pos = w_pos[li];
+#pragma unroll
+            for (int sl = 0; sl < RPT; sl++) {
+                if (sl >= rpt) break;
+                uint4 ctr = ctr0;
+                ctr.x = (uint32_t)pos;
+                ctr.w |= W_WIDE | ((uint32_t)sl << 8);
+                const double num = (lj > NORMAL_THRESH) ? normal_draw(ctr, a.key, lj) : ptrs64(ctr, a.key, lj, d_status);
+                if (!SORTED || pos >= __ldg(q_row + sl * RB)) acc[sl] += num * hj;
+            }
+        }
+    }
+    if (!any) return;
+#pragma unroll
+    for (int i = 0; i < RPT; i++)
+        if (i < rpt) part[((long)c * a.nf + f) * a.nr + r0 + (long)i * RB] += acc[i];
 }
 
 // ---- 5. background = prefix remainder + chunk partials (fixed order)
@@ -1405,6 +1602,8 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
     k_bulk<true, false><<<grid, RB, 0, st>>>(a, ParArgs{}, lam_s, h_s, q, part, d_status);
     if ((rc = hgb::check_launch())) return rc;
     if ((rc = bulk_event(1, st))) return rc;
+    k_bulk_wide<true><<<grid, RB, 0, st>>>(a, lam_s, h_s, q, part, d_status);
+    if ((rc = hgb::check_launch())) return rc;
     k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, bgp, part, hc2bg);
     return hgb::check_launch();
 }
@@ -1531,6 +1730,8 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     k_bulk<false, false><<<grid, RB, 0, st>>>(a, ParArgs{}, number, hc2, nullptr, (double *)workspace, d_status);
     int rc = hgb::check_launch();
     if (rc) return rc;
+    k_bulk_wide<false><<<grid, RB, 0, st>>>(a, number, hc2, nullptr, (double *)workspace, d_status);
+    if ((rc = hgb::check_launch())) return rc;
     long nfr = (long)n_freq * nreals;
     k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, nullptr, (double *)workspace, gwb);
     return hgb::check_launch();

@@ -235,7 +235,7 @@ def test_philox_poisson_statistics(built_lib):
     """Counts of the Philox sampler follow Poisson(lambda) across all sampler regimes."""
     from holodeck_gb300 import cyutils
     from scipy import stats
-    lams = np.array([1e-7, 0.03, 0.12, 0.16, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 6.0e4, 9.1e4, 5.0e6])
+    lams = np.array([1e-7, 0.03, 0.099, 0.1, 0.12, 0.16, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 6.0e4, 9.1e4, 5.0e6])
     nreals = 20000
     # one bin per lambda, one frequency; L=0 so every source goes to the background sum
     number = lams.reshape(-1, 1, 1, 1)
@@ -253,6 +253,11 @@ def test_philox_poisson_statistics(built_lib):
         assert abs(mean - lam) < 5 * se + 1e-12, (lam, mean)
         if lam > 0.01:
             assert abs(var / lam - 1.0) < 5 * np.sqrt(2.0 / nreals) * max(1.0, 1.0 / np.sqrt(lam)) + 0.02, (lam, var)
+        if 0.02 < lam <= 0.5:   # geometric skipping and the small tables near their boundary
+            obs = np.array([(cnt == 0).sum(), (cnt == 1).sum(), (cnt >= 2).sum()])
+            exp = np.array([stats.poisson.pmf(0, lam), stats.poisson.pmf(1, lam), stats.poisson.sf(1, lam)]) * nreals
+            chi2 = ((obs - exp) ** 2 / exp).sum()
+            assert stats.chi2.sf(chi2, 2) > 1e-4, (lam, obs, exp)
         if 0.5 < lam < 1e3:
             lo, hi = int(stats.poisson.ppf(1e-4, lam)), int(stats.poisson.ppf(1 - 1e-4, lam))
             ks = np.arange(lo, hi + 1)
