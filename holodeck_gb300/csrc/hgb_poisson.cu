@@ -70,7 +70,7 @@ namespace {
 constexpr int RB = 128;                  // threads per block == bins per staged tile
 constexpr int NWARP = RB / 32;
 constexpr int RPT = 8;                   // realizations per thread
-static_assert(RPT % 4 == 0, "the table passes draw four realizations per Philox call");
+static_assert(RPT == 8, "the table passes draw four realizations per Philox call, two calls per bin");
 constexpr int NT = 32;                   // CDF thresholds per small-lambda bin
 constexpr double SPARSE_MAX = 0.1;       // geometric skipping over realizations below this expectation
 constexpr double NORMAL_THRESH = 1e10;   // long(1e10) in cyutils.pyx:1223
@@ -85,6 +85,8 @@ constexpr int TMAX = 4096;               // table entries (>= 14 * 256 + 9)
 constexpr int ARENA_WORDS = TMAX + TMAX / 2;   // one largest table: cdf words + u16 guide cells
 constexpr int HALF_WORDS = ARENA_WORDS / 2;   // the arena's halves alternate between build and draw
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
+constexpr unsigned GUIDE_PURE = 0x8000u, GUIDE_ONE = 0x4000u, GUIDE_M = 0x0FFFu;   // guide cell fields
+static_assert(TMAX - 1 <= (int)GUIDE_M, "table entries fit the guide's index field");
 constexpr int ANCHOR = 8;                // Loader-form pmf every ANCHOR-th entry, the recursion between
 constexpr float TABLE_SIGMAS = 7.0f;     // the table covers lambda +- 7 sqrt(lambda) (tails < 1e-11)
 // draw families (counter .w high bits)
@@ -673,8 +675,12 @@ struct BulkArgs {
 //   cdf[m]   = min(sum of q(k_lo) .. q(k_lo + m), 2^32 - 1), with q(k) = P(k) in 32.32 fixed point
 //              (rounded to nearest); cdf[S - 1] = 2^32 - 1, so the mass outside the range (< 1e-11)
 //              goes to the end entries;
-//   guide[c] = smallest m with cdf[m] > c 2^(32 - gb), for the 2^gb >= S cells, with bit 15 set when
-//              cdf[m] >= (c + 1) 2^(32 - gb): every u in the cell then maps to m ("pure" cell).
+//   guide[c] = m | flags, m (bits 0-11) the smallest entry with cdf[m] > c 2^(32 - gb), for the
+//              2^gb >= S cells; GUIDE_PURE when cdf[m] >= (c + 1) 2^(32 - gb), so every u in the cell
+//              maps to m; GUIDE_ONE when instead cdf[m + 1] >= (c + 1) 2^(32 - gb), so u maps to m or
+//              m + 1 by one comparison; neither: two or more entries end inside the cell (a "tail"
+//              cell of the distribution), resolved by a binary search between guide[c] and
+//              guide[c + 1].
 // P(k) is FP32: the Loader form at every ANCHOR-th entry and the recursion P(k) = P(k-1) lambda / k
 // in between (__fdividef: at most 2 ulp per step, so under 16 ulp of drift before the next anchor).
 // Each thread takes E consecutive entries; the guide is the merge of the cdf values with the cell
@@ -736,13 +742,17 @@ __device__ __forceinline__ void table_guide(const unsigned int *cdf, unsigned sh
         else hi = mid;
     }
     int m = lo, c = d0 - lo;
-    unsigned am = cdf[min(m, S - 1)];
+    unsigned am = cdf[min(m, S - 1)], an = cdf[min(m + 1, S - 1)];   // cdf[m] and cdf[m + 1]
     for (int d = d0; d < d1 && c < nc; d++) {
         if (am <= ((unsigned)c << shift)) {   // m < S - 1: cdf[S - 1] = 2^32 - 1 exceeds every cell start
             m++;
-            am = cdf[m];
+            am = an;
+            an = cdf[min(m + 1, S - 1)];
         } else {
-            guide[c] = (unsigned short)(m | ((am >> shift) > (unsigned)c ? 0x8000 : 0));
+            unsigned code = (unsigned)m;
+            if ((am >> shift) > (unsigned)c) code |= GUIDE_PURE;
+            else if (m + 1 < S && (an >> shift) > (unsigned)c) code |= GUIDE_ONE;
+            guide[c] = (unsigned short)code;
             c++;
         }
     }
@@ -1022,7 +1032,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                     const int j = s.list[KIND_TABLE][cur_li + i];
                     const int pos = s.pos[j];
                     const float hs = s.hs[j];
-                    const int k_lo = s.tb_klo[j], S = s.tb_S[j], shift = 32 - s.tb_gb[j];
+                    const int k_lo = s.tb_klo[j], S = s.tb_S[j], gb = s.tb_gb[j], shift = 32 - gb;
                     const unsigned int *cdf = s.u.arena + off;
                     const unsigned short *guide = (const unsigned short *)(s.u.arena + off + S);
                     off += table_words(s, j);
@@ -1034,6 +1044,11 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                         ctr.w |= W_TABLE | (uint32_t)call;
                         wv[call] = philox(ctr, a.key);
                     }
+                    // Straight-line lookups (no data-dependent branch, so the eight draws
+                    // interleave): a pure cell answers from the guide, a one-boundary cell with one
+                    // comparison.  Draws in tail cells (a few percent) are marked and finished after
+                    // the bin's other draws by a binary search inside the cell.
+                    unsigned pend = 0;
 #pragma unroll
                     for (int call = 0; call < RPT / 4; call++) {
                         if (4 * call >= rpt) break;
@@ -1045,12 +1060,38 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                             if (sl >= rpt) continue;
                             const uint32_t uc = min(u, 0xFFFFFFFEu);   // below cdf[S - 1]
                             const unsigned g = guide[uc >> shift];
-                            int e = (int)(g & 0x7FFFu);
-                            if (!(g & 0x8000u))
-                                while (uc >= cdf[e]) e++;
-                            if (!check || pos >= __ldg(q_row + sl * RB)) {
+                            int e = (int)(g & GUIDE_M);
+                            if (g & GUIDE_ONE) e += (uc >= cdf[e]) ? 1 : 0;
+                            const bool tail = !(g & (GUIDE_PURE | GUIDE_ONE));
+                            pend |= tail ? (1u << sl) : 0u;
+                            if (!tail && (!check || pos >= __ldg(q_row + sl * RB))) {
                                 kahan_add(acc_r[sl], comp_r[sl], (float)(k_lo + e) * hs);
                                 if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + e));
+                            }
+                        }
+                    }
+                    if (__any_sync(0xffffffffu, pend != 0)) {
+                        // the lane's tail draws in turn; their slot is data dependent, so the sums
+                        // go to the shared-memory Kahan accumulators
+#pragma unroll 1
+                        while (pend) {
+                            const int sl = __ffs(pend) - 1;
+                            pend &= pend - 1;
+                            const uint4 w = (sl < 4) ? wv[0] : wv[RPT / 4 - 1];
+                            const int q4 = sl & 3;
+                            const uint32_t u = (q4 == 0) ? w.x : (q4 == 1) ? w.y : (q4 == 2) ? w.z : w.w;
+                            const uint32_t uc = min(u, 0xFFFFFFFEu);
+                            const unsigned cell = uc >> shift;
+                            int lo = (int)(guide[cell] & GUIDE_M);
+                            int hi = (cell + 1 < (1u << gb)) ? (int)(guide[cell + 1] & GUIDE_M) : S - 1;
+                            while (lo < hi) {   // cdf[hi] > uc throughout
+                                const int mid = (lo + hi) >> 1;
+                                if (uc >= cdf[mid]) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            if (!check || pos >= __ldg(q_row + sl * RB)) {
+                                add_bg(st, sl, t, (float)(k_lo + lo) * hs);
+                                if (PARAMS) add_par(psm, sl, t, j, (float)(k_lo + lo));
                             }
                         }
                     }
