@@ -38,9 +38,8 @@
 //                             zero-truncated Poisson.  The block's realizations are cut into runs of
 //                             2^lg (about one expected event each) and one thread walks a run, so a
 //                             bin costs about one draw per event instead of one per lane
-//   SPARSE_MAX <= lambda < 10 inversion of a 32-bit uniform against the bin's table of
-//                             floor(CDF(n) 2^32), n < 32, by a branch-free binary search; four
-//                             realizations per Philox call
+//   SPARSE_MAX <= lambda < 10 a 32-column alias row per bin (n < 31 and the rest at 31): one
+//                             lookup and one comparison per draw; four realizations per Philox call
 //   10 <= lambda <= 65536     inversion against a per-bin table over lambda +- 7 sqrt(lambda) in
 //                             shared memory, with a guide table whose "pure" cells answer most draws
 //                             with one lookup; four realizations per Philox call
@@ -167,8 +166,8 @@ __constant__ float c_invf[NT] = {
 // small-lambda pass finishes before the first table is built.
 struct Tile {
     union {
-        // small lambda: floor(CDF(n) 2^32), n = 0..31, one padded row per bin: the lanes of a warp
-        // search one bin's row at different n, which the padding puts in different banks
+        // small lambda: one padded 32-column alias row per bin (threshold << 5 | alias); the lanes of
+        // a warp read one bin's row at different columns, which the padding puts in different banks
         unsigned int thr[RB][NT + 1];
         unsigned int arena[ARENA_WORDS];          // table kind: packed cdf (u32) + guide (u16) tables
     } u;
@@ -218,22 +217,55 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
         s.lamf[j] = lf;
         s.sp_lg[j] = (unsigned char)(lf > 0.0f ? max(3, min(10, -ilogbf(lf) - 1)) : 10);
     } else if (kind == KIND_SMALL) {
-        // P(n) in FP32 by the recursion P(n) = P(n-1) lambda / n, rounded to 32.32 fixed point and
-        // summed exactly; the last threshold is saturated (P(n >= 31) < 1e-8 for lambda < 10)
+        // q(n) = P(n) in FP32 by the recursion P(n) = P(n-1) lambda / n, rounded to 32.32 fixed point,
+        // for n < 31; n = 31 carries the rest (P(n >= 31) < 2e-9 for lambda < 10; a rounding excess
+        // comes off the mode instead), so sum q = 2^32.  Then a 32-column alias row (Walker 1977,
+        // each column 2^27 of the 2^32 units) by the sweep over lights and heavies in index order:
+        // word = threshold (27 bits) << 5 | alias (5 bits).
+        unsigned *row = s.u.thr[j];
         const float lf = (float)lam;
         float p = expf(-lf);
         unsigned long long cum = 0;
-        int n = 0;
-        for (; n < NT - 1; n++) {
+        unsigned qmax = 0;
+        int mode = 0;
+        for (int n = 0; n < NT - 1; n++) {
             if (n > 0) p = p * lf * c_invf[n];
-            cum += __float2uint_rn(p * 0x1.0p32f);
-            s.u.thr[j][n] = (cum < 0xFFFFFFFFull) ? (unsigned int)cum : 0xFFFFFFFFu;
-            if ((float)n > lf && p < 0x1.0p-34f) {
-                n++;
-                break;
+            const unsigned q = __float2uint_rn(p * 0x1.0p32f);
+            row[n] = q;
+            cum += q;
+            if (q > qmax) {
+                qmax = q;
+                mode = n;
             }
         }
-        for (; n < NT; n++) s.u.thr[j][n] = 0xFFFFFFFFu;
+        if (cum <= 0x100000000ull) {
+            row[NT - 1] = (unsigned)(0x100000000ull - cum);   // cum > 0: q(0) > 0
+        } else {
+            row[mode] -= (unsigned)(cum - 0x100000000ull);
+            row[NT - 1] = 0u;
+        }
+        constexpr unsigned C = 1u << 27;
+        unsigned heavy = 0;
+        for (int n = 0; n < NT; n++)
+            if (row[n] >= C) heavy |= 1u << n;
+        int jh = __ffs(heavy) - 1;   // a heavy exists: the 32 entries sum to 32 C
+        unsigned rest = heavy & (heavy - 1);
+        unsigned r = row[jh];
+        for (int n = 0; n < NT; n++) {
+            if (heavy >> n & 1) continue;
+            const unsigned qn = row[n];
+            row[n] = (qn << 5) | (unsigned)jh;
+            r -= C - qn;
+            while (r < C && rest) {   // heavy jh is used up: its own column, aliased to the next
+                const int jn = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const unsigned qj = row[jn];
+                row[jh] = (r << 5) | (unsigned)jn;
+                r = qj - (C - r);
+                jh = jn;
+            }
+        }
+        row[jh] = ((C - 1) << 5) | (unsigned)jh;   // the last heavy keeps its whole column
     } else if (kind == KIND_TABLE || kind == KIND_PTRS32) {
         const float lf = (float)lam;
         const double li = floor(lam);
@@ -387,25 +419,6 @@ __device__ int truncated_count_f32(float lam, float v, int *d_status) {
     return n;
 }
 
-// Count of a small-lambda bin beyond its 32-entry table (P < 1e-8 for lambda < 10).
-__device__ int small_tail(double lam, uint32_t u, int *d_status) {
-    double uu = ((double)u + 0.5) * 0x1.0p-32;
-    double p = exp(-lam);
-    double cdf = p;
-    int m = 0;
-    while (uu >= cdf) {
-        if (m >= MAX_INVERSION) {
-            hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-            break;
-        }
-        m++;
-        p *= lam / m;
-        const double next = cdf + p;
-        if (next == cdf) break;
-        cdf = next;
-    }
-    return m < NT ? NT : m;
-}
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
     float y = x - comp;
@@ -930,7 +943,6 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
             const int pos = s.pos[j];
             const float hs = s.hs[j];
             const unsigned int *row = s.u.thr[j];
-            const unsigned int t0 = row[0];
             uint4 wv[RPT / 4];   // every call issued first: independent round chains interleave
 #pragma unroll
             for (int call = 0; call < RPT / 4; call++) {
@@ -947,15 +959,11 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
                 for (int m = 0; m < 4; m++) {
                     const int sl = 4 * call + m;
                     const uint32_t u = (m == 0) ? w.x : (m == 1) ? w.y : (m == 2) ? w.z : w.w;
-                    if (sl >= rpt || u < t0) continue;
-                    int n = 0;
-                    if (u >= row[n + 15]) n += 16;
-                    if (u >= row[n + 7]) n += 8;
-                    if (u >= row[n + 3]) n += 4;
-                    if (u >= row[n + 1]) n += 2;
-                    if (u >= row[n]) n += 1;
-                    if (n == NT - 1 && u >= row[NT - 1]) n = small_tail(s.lam[j], u, d_status);
-                    if (!check || pos >= __ldg(q_row + sl * RB)) {
+                    if (sl >= rpt) continue;
+                    // column u >> 27, fraction the low 27 bits: P(n) = q(n) / 2^32 exactly
+                    const unsigned wd = row[u >> 27];
+                    const int n = ((u & 0x07FFFFFFu) < (wd >> 5)) ? (int)(u >> 27) : (int)(wd & 31u);
+                    if (n != 0 && (!check || pos >= __ldg(q_row + sl * RB))) {
                         kahan_add(acc_r[sl], comp_r[sl], (float)n * hs);
                         if (PARAMS) add_par(psm, sl, t, j, (float)n);
                     }
