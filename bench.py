@@ -192,7 +192,7 @@ def run_gpu(args):
     # strain of the bins with a nonzero expectation (8 B each), each realization's first bulk
     # position read, the per-chunk partials written
     n_rgroups = -(-NREALS // 1024)
-    nchunk = max(1, -(-152 * 5 * 2 // (NFREQ * n_rgroups)))
+    nchunk = max(1, -(-152 * 6 * 2 // (NFREQ * n_rgroups)))
     n_pos = int((number > 0).sum().item())
     alg_bytes = (8 * nb * NFREQ + 8 * n_pos) * n_rgroups + 4 * NFREQ * NREALS + 8 * nchunk * NFREQ * NREALS
     peaks = {}

@@ -62,6 +62,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "hgb_common.cuh"
 
 namespace {
@@ -79,13 +81,14 @@ constexpr int MAX_ATTEMPTS = 64;
 constexpr int MAX_PTRS_ITERS = 2 * RPT + 64;   // attempts of one lane over its RPT realizations
 constexpr int MAX_INVERSION = 4096;
 constexpr int MAX_PREFIX_EXTRA = 1024;   // prefix events beyond L (Normal draws below 1)
-constexpr double TABLE_MAX = 65536.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 9
-constexpr int TMAX = 4096;               // table entries (>= 14 * 256 + 9)
-constexpr int ARENA_WORDS = TMAX + TMAX / 2;   // one largest table: cdf words + u16 guide cells
-constexpr int HALF_WORDS = ARENA_WORDS / 2;   // the arena's halves alternate between build and draw
+constexpr double TABLE_MAX = 11500.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 9
+constexpr int TMAX = 1536;               // table entries (>= 14 sqrt(TABLE_MAX) + 9 = 1510)
+constexpr int HALF_WORDS = TMAX + 1024;  // the largest table: TMAX cdf words + 2^11 u16 guide cells
+constexpr int ARENA_WORDS = 2 * HALF_WORDS;   // the halves alternate between build and draw
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
 constexpr unsigned GUIDE_PURE = 0x8000u, GUIDE_ONE = 0x4000u, GUIDE_M = 0x0FFFu;   // guide cell fields
 static_assert(TMAX - 1 <= (int)GUIDE_M, "table entries fit the guide's index field");
+static_assert(ARENA_WORDS >= RB * (NT + 1), "the small-lambda rows share the arena");
 constexpr int ANCHOR = 8;                // Loader-form pmf every ANCHOR-th entry, the recursion between
 constexpr float TABLE_SIGMAS = 7.0f;     // the table covers lambda +- 7 sqrt(lambda) (tails < 1e-11)
 // draw families (counter .w high bits)
@@ -192,9 +195,14 @@ __device__ __forceinline__ int kind_count(const Tile &s, int k) {
     return n;
 }
 
-// Per-realization state of a block for the passes whose realization index is data dependent,
-// indexed [slot][thread].
-struct Slots {
+// Per-realization sums of a block for the passes whose realization slot is data dependent (table
+// tail cells, PTRS, and with the parameter sums every per-lane pass), indexed [slot][thread]:
+// plain FP32 where the terms are few (a few percent of the table draws and the PTRS bins), Kahan
+// pairs for the parameter path.
+struct SlotsPlain {
+    float acc[RPT][RB];
+};
+struct SlotsKahan {
     float acc[RPT][RB];
     float comp[RPT][RB];
 };
@@ -427,7 +435,17 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
     sum = t;
 }
 
-__device__ __forceinline__ void add_bg(Slots &st, int sl, int t, float x) {
+__device__ __forceinline__ void add_bg(SlotsPlain &st, int sl, int t, float x) { st.acc[sl][t] += x; }
+__device__ __forceinline__ void slot_zero(SlotsPlain &st, int sl, int t) { st.acc[sl][t] = 0.0f; }
+__device__ __forceinline__ double slot_value(const SlotsPlain &st, int sl, int t) { return (double)st.acc[sl][t]; }
+__device__ __forceinline__ void slot_zero(SlotsKahan &st, int sl, int t) {
+    st.acc[sl][t] = 0.0f;
+    st.comp[sl][t] = 0.0f;
+}
+__device__ __forceinline__ double slot_value(const SlotsKahan &st, int sl, int t) {
+    return (double)st.acc[sl][t] - (double)st.comp[sl][t];
+}
+__device__ __forceinline__ void add_bg(SlotsKahan &st, int sl, int t, float x) {
     float acc = st.acc[sl][t], comp = st.comp[sl][t];
     kahan_add(acc, comp, x);
     st.acc[sl][t] = acc;
@@ -841,12 +859,12 @@ __device__ __forceinline__ void add_par(float *psm, int sl, int t, int j, float 
 }
 
 template <bool SORTED, bool PARAMS>
-__global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
+__global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
                                                           const double *__restrict__ h_in,
                                                           const int *__restrict__ qpos, double *__restrict__ part,
                                                           int *d_status) {
     __shared__ Tile s;
-    __shared__ Slots st;
+    __shared__ typename std::conditional<PARAMS, SlotsKahan, SlotsPlain>::type st;
     extern __shared__ float psm[];   // PARAMS only: PAR_SMEM bytes
     __shared__ int q_min_s, q_max_s;
     const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
@@ -861,8 +879,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
     for (int i = 0; i < RPT; i++) {
         acc_r[i] = 0.0f;
         comp_r[i] = 0.0f;
-        st.acc[i][t] = 0.0f;
-        st.comp[i][t] = 0.0f;
+        slot_zero(st, i, t);
         int q = 0x7FFFFFFF;
         if (i < rpt) q = SORTED ? qpos[(long)f * a.nr + r0 + i * RB] : 0;
         if (i < rpt) {
@@ -1297,7 +1314,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 5) k_bulk(BulkArgs a, ParArgs
     for (int i = 0; i < RPT; i++)
         if (i < rpt)
             part[((long)c * a.nf + f) * a.nr + r0 + (long)i * RB] =
-                (((double)acc_r[i] - (double)comp_r[i]) + ((double)st.acc[i][t] - (double)st.comp[i][t])) * HSCALE_INV;
+                (((double)acc_r[i] - (double)comp_r[i]) + slot_value(st, i, t)) * HSCALE_INV;
     if (PARAMS) {
         const float *pacc = psm + NPAR * RB;
         const float *pcomp = pacc + NPAR * RPT * RB;
@@ -1490,7 +1507,7 @@ int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
 int choose_nchunk(long nb, int nf, int nr) {
     long blocks = (long)n_rgroups(nr) * nf;
-    long target = 152L * 5 * 2;   // two waves of resident blocks on 152 SMs
+    long target = 152L * 6 * 2;   // two waves of resident blocks (six per SM) on 152 SMs
     long nchunk = hgb::ceil_div(target, blocks);
     long maxc = hgb::ceil_div(nb, 8L * RB);
     if (nchunk > maxc) nchunk = maxc;
