@@ -9,6 +9,8 @@ find the hardening normalisation, and gwb() (dynamic binary number, integration,
 Poisson realizations with the loudest split).  value = realizations / s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --stages        # per-stage device times
+    python bench.py --profile --nfreqs K   # one untimed evaluation (the program ncu captures)
 
 --impl reference times the CPU restatement of the reference path (the oracle) on the host cores.
 """
@@ -353,6 +355,44 @@ def run_profile(args):
     print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1}))
 
 
+def run_stages(args):
+    """Device time of each stage of one model evaluation (CUDA events on the current stream), median
+    over ``--steps`` evaluations after ``--warmup``: the breakdown behind the headline number.  The
+    hardening normalisation starts on a side stream when the hardening model is built and overlaps
+    the density; hardening_norm_wait is what is left of it afterwards."""
+    import torch
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    from holodeck_gb300 import single_sources
+    _, fe = H.utils.pta_freqs(16.0 * C.YR, NFREQ)
+    fo_c = H.utils.midpoints(fe) / 2.0
+    names = ["density_and_scatter", "hardening_norm_wait", "dbn", "number_and_strain", "sort", "realizations"]
+    rows = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+        ev[0].record()
+        sam, hard = make_model(H, C)
+        sam._density_device()
+        ev[1].record()
+        hard._norm_device()
+        ev[2].record()
+        redz_final, diff_num = sam._dbn_device(hard, fo_c)
+        ev[3].record()
+        number, h2fdf = sam._number_and_strain(fe / 2.0, diff_num, redz_final)
+        ev[4].record()
+        order = single_sources.sort_order_device(h2fdf)
+        ev[5].record()
+        single_sources.ss_realize_device(number, h2fdf, NREALS, NLOUD, seed=i, order=order)
+        ev[6].record()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            rows.append([ev[k].elapsed_time(ev[k + 1]) for k in range(len(names))])
+    med = [statistics.median(r[k] for r in rows) for k in range(len(names))]
+    print(json.dumps({"stages_ms": dict(zip(names, [round(m, 3) for m in med])), "sum_ms": round(sum(med), 3),
+                      "config": {"workload": CONFIG_NAME}, "evaluations": args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,9 +402,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="run warmup + 1 untimed evaluations (for ncu)")
     ap.add_argument("--nfreqs", type=int, default=NFREQ, help="frequencies of a --profile run")
+    ap.add_argument("--stages", action="store_true", help="per-stage device times of one model evaluation")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+    elif args.stages:
+        run_stages(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
