@@ -89,7 +89,7 @@ constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
 constexpr unsigned GUIDE_PURE = 0x8000u, GUIDE_ONE = 0x4000u, GUIDE_M = 0x0FFFu;   // guide cell fields
 static_assert(TMAX - 1 <= (int)GUIDE_M, "table entries fit the guide's index field");
 static_assert(ARENA_WORDS >= RB * (NT + 1), "the small-lambda rows share the arena");
-constexpr int ANCHOR = 8;                // Loader-form pmf every ANCHOR-th entry, the recursion between
+constexpr int ANCHOR = 16;               // Loader-form pmf every ANCHOR-th entry, the recursion between
 constexpr float TABLE_SIGMAS = 7.0f;     // the table covers lambda +- 7 sqrt(lambda) (tails < 1e-11)
 // draw families (counter .w high bits)
 constexpr uint32_t W_SMALL = 0x00000000u;   // | call: 4 realizations per call
@@ -304,21 +304,23 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
 }
 
 // bd0(k, lambda) = k log(k / lambda) + lambda - k (Loader 2000) in FP32 from d = k - lambda, which
-// the caller forms exactly as (k - floor(lambda)) - frac(lambda).
+// the caller forms exactly as (k - floor(lambda)) - frac(lambda).  The quotients use __fdividef
+// (2 ulp): bd0 then carries a relative error of a few 1e-7, which moves exp(-bd0) by at most about
+// 5e-6 relative in the far tails (bd0 ~ 25, P ~ 1e-11) and about 1e-7 near the mode.
 __device__ __forceinline__ float bd0_f32(float kk, float d, float lamf) {
-    const float v = d / (kk + lamf);
+    const float v = __fdividef(d, kk + lamf);
     if (fabsf(v) < 0.1f) {
         const float v2 = v * v;
         return d * v + 2.0f * kk * v * v2 * (0.33333333f + v2 * (0.2f + v2 * (0.14285714f + v2 * 0.11111111f)));
     }
-    return kk * log1pf(d / lamf) - d;
+    return kk * log1pf(__fdividef(d, lamf)) - d;
 }
 
 __device__ __forceinline__ float stirlerr_f32(int k) {
     if (k < 16) return c_stirl[k];
     const float kk = (float)k;
-    const float ik2 = 1.0f / (kk * kk);
-    return (0.083333333333f - (0.0027777777778f - 0.00079365079365f * ik2) * ik2) / kk;
+    const float ik2 = __fdividef(1.0f, kk * kk);
+    return __fdividef(0.083333333333f - (0.0027777777778f - 0.00079365079365f * ik2) * ik2, kk);
 }
 
 // P(k; lambda) in FP32, relative error ~1e-7 across the table range:
@@ -713,7 +715,7 @@ struct BulkArgs {
 //              cell of the distribution), resolved by a binary search between guide[c] and
 //              guide[c + 1].
 // P(k) is FP32: the Loader form at every ANCHOR-th entry and the recursion P(k) = P(k-1) lambda / k
-// in between (__fdividef: at most 2 ulp per step, so under 16 ulp of drift before the next anchor).
+// in between (__fdividef: at most 2 ulp per step, so under 32 ulp of drift before the next anchor).
 // Each thread takes E consecutive entries; the guide is the merge of the cdf values with the cell
 // starts, split evenly over the threads (merge path), so no thread waits on another's long run of
 // cells or entries.
