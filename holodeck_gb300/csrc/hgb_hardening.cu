@@ -32,9 +32,16 @@ constexpr int BRENT_MAXITER = 100;
 // hardening normalisation
 // ------------------------------------------------------------------------------------------------
 
+struct PowPlan {
+    int kind;   // 0: pow(), 1: integer, 2: half-integer
+    int n;      // |y| rounded down
+    int neg;    // y < 0
+};
+
 struct NormArgs {
     double target_time, sepa_init_log10, rchar, gi, go;
     int nsteps;
+    PowPlan p_outer, p_inner;   // exponents -go + gi and gi - 1 of the hardening rate
 };
 
 // Lifetime minus target for one cell, evaluated by the whole warp (sam_cyutils.pyx:360-398).
@@ -172,12 +179,6 @@ __global__ void k_hardening_norm(CyConst cc, NormArgs a, const double *__restric
 // x^y for an exponent fixed per call.  Integer and half-integer exponents up to |y| = 8.5 (the
 // hardening model's defaults give -3.5 and -2) are evaluated as products and one square root,
 // within a few ulp of pow(); any other exponent goes to pow().
-struct PowPlan {
-    int kind;   // 0: pow(), 1: integer, 2: half-integer
-    int n;      // |y| rounded down
-    int neg;    // y < 0
-};
-
 PowPlan pow_plan(double y) {
     PowPlan p{0, 0, y < 0.0};
     const double ay = fabs(y), twice = 2.0 * ay;
@@ -246,11 +247,18 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
         }
     }
     __syncthreads();
+    // per node: sp^1.5 as sp sqrt(sp), the hardening model's (half-)integer powers as products
+    // (pow_planned), and the GW rate with the cell's mt^3 and (1 + mr)^2 taken once: each within a
+    // few ulp of the pow() forms of sam_cyutils.pyx:240-253 and holodeck/cyutils.pyx
+    const double sqrt_mt = sqrt(mt), mt3 = pow(mt, 3.0), mr12 = pow(1.0 + mr, 2.0);
     for (int s = threadIdx.x; s <= S; s += blockDim.x) {
-        double sp = pow(10.0, sepa[s]);
+        const double sp = pow(10.0, sepa[s]);
         sepa[s] = sp;
-        frst[s] = cc.kfreq * sqrt(mt) / pow(sp, 1.5);
-        dadt[s] = hgb::hard_func_2pwl_gw(cc.c_dadt, mt, mr, sp, norm, a.rchar, a.gi, a.go);
+        frst[s] = cc.kfreq * sqrt_mt / (sp * sqrt(sp));
+        const double xx = sp / a.rchar;
+        double dd = -norm * pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
+        dd += cc.c_dadt * mt3 * mr / (sp * sp * sp) / mr12;
+        dadt[s] = dd;
     }
     __syncthreads();
     for (int s = threadIdx.x; s < S; s += blockDim.x) dts[s] = 2.0 * (sepa[s + 1] - sepa[s]) / (dadt[s] + dadt[s + 1]);
@@ -496,6 +504,7 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
     double *myc = crow + (size_t)warp * (S + 1);
     double *mydt = dts + (size_t)warp * S;
     const double mt = valid ? mtot[cell] : 1.0, mr = valid ? mrat[cell] : 1.0;
+    const double mt3 = pow(mt, 3.0), mr12 = pow(1.0 + mr, 2.0);
     // log10 separation nodes by repeated subtraction (sam_cyutils.pyx:367-383), one lane per cell
     if (warp == 0 && lane < NB_CELLS) {
         const int c = blockIdx.x * NB_CELLS + lane;
@@ -512,18 +521,19 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
         }
     }
     __syncthreads();
-    double aa[NB_NODES], bb[NB_NODES], gw[NB_NODES], sp[NB_NODES];
+    // per node: the hardening shape (1 + x)^(gi - go) / x^(gi - 1) and the GW rate, which do not
+    // depend on the normalisation, so each Brent round costs one product and one sum per node
+    double rr[NB_NODES], gw[NB_NODES], sp[NB_NODES];
 #pragma unroll
     for (int k = 0; k < NB_NODES; k++) {
         const int s = lane + 32 * k;
-        aa[k] = bb[k] = 1.0;
+        rr[k] = 1.0;
         gw[k] = sp[k] = 0.0;
         if (valid && s <= S) {
             const double x = pow(10.0, myc[s]);
             const double xx = x / a.rchar;
-            aa[k] = pow(1.0 + xx, -a.go + a.gi);
-            bb[k] = pow(xx, a.gi - 1.0);
-            gw[k] = hgb::hard_gw(cc.c_dadt, mt, mr, x);
+            rr[k] = pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
+            gw[k] = cc.c_dadt * mt3 * mr / (x * x * x) / mr12;
             sp[k] = x;
         }
     }
@@ -551,7 +561,7 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
             double v[NB_NODES];
 #pragma unroll
             for (int k = 0; k < NB_NODES; k++) {
-                double dl = -nrm * aa[k] / bb[k];
+                double dl = -nrm * rr[k];
                 dl += gw[k];
                 v[k] = dl;
             }
@@ -689,7 +699,8 @@ int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const d
             return HGB_ERR_CUDA;
         }
     }
-    NormArgs a{target_time, log10(sepa_init), rchar, gamma_inner, gamma_outer, nsteps};
+    NormArgs a{target_time, log10(sepa_init), rchar, gamma_inner, gamma_outer, nsteps,
+               pow_plan(-gamma_outer + gamma_inner), pow_plan(gamma_inner - 1.0)};
     if (nsteps + 1 <= 32 * NB_NODES) {
         const size_t bsmem = norm_blk_smem(nsteps);
         cudaError_t err = cudaFuncSetAttribute(k_hardening_norm_blk, cudaFuncAttributeMaxDynamicSharedMemorySize,
