@@ -91,6 +91,27 @@ __device__ __forceinline__ double comoving_distance(const double *dval, const do
     return h00 * dval[k] + h10 * h * dder[k] + h01 * dval[k + 1] + h11 * h * dder[k + 1];
 }
 
+// The same lookup for z >= 0 with u = (1 + z)^(-1/2) from an FP32 estimate and one FP64 Newton
+// step, u (3 - y u^2) / 2 (relative error about 1e-14, far below the table's own), and h = 1 / n
+// supplied by the caller: about a third of the FP64 work of comoving_distance.
+__device__ __forceinline__ double comoving_distance_fast(const double *dval, const double *dder, int n, double h,
+                                                         double z) {
+    const double y = 1.0 + z;
+    const double u0 = (double)rsqrtf((float)y);
+    const double u = u0 * (3.0 - y * (u0 * u0)) * 0.5;
+    double x = u * (double)n;
+    int k = (int)x;
+    if (k >= n) k = n - 1;
+    if (k < 0) k = 0;
+    double t = x - (double)k;
+    double t2 = t * t, t3 = t2 * t;
+    double h00 = 2.0 * t3 - 3.0 * t2 + 1.0;
+    double h10 = t3 - 2.0 * t2 + t;
+    double h01 = -2.0 * t3 + 3.0 * t2;
+    double h11 = t3 - t2;
+    return h00 * dval[k] + h10 * h * dder[k] + h01 * dval[k + 1] + h11 * h * dder[k + 1];
+}
+
 __host__ __device__ __forceinline__ long ceil_div(long a, long b) { return (a + b - 1) / b; }
 
 }  // namespace hgb

@@ -196,6 +196,18 @@ __device__ __forceinline__ double pow_planned(double x, double y, PowPlan p) {
     return p.neg ? 1.0 / r : r;
 }
 
+// x1^y1 / x2^y2 with both exponents planned: the two magnitudes as products and square roots and
+// at most one division (within a few ulp of the quotient of the pow() forms)
+__device__ __forceinline__ double pow_ratio_planned(double x1, double y1, PowPlan p1, double x2, double y2,
+                                                   PowPlan p2) {
+    if (p1.kind == 0 || p2.kind == 0) return pow_planned(x1, y1, p1) / pow_planned(x2, y2, p2);
+    double r1 = (p1.kind == 2) ? sqrt(x1) : 1.0, r2 = (p2.kind == 2) ? sqrt(x2) : 1.0;
+    for (int i = 0; i < p1.n; i++) r1 *= x1;
+    for (int i = 0; i < p2.n; i++) r2 *= x2;
+    if (p1.neg) return p2.neg ? r2 / r1 : 1.0 / (r1 * r2);
+    return p2.neg ? r1 * r2 : r1 / r2;
+}
+
 struct Dbn2plArgs {
     double sepa_init_log10, rchar, gi, go;
     int num_steps, n_freq, fobs_sorted;
@@ -256,7 +268,7 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
         sepa[s] = sp;
         frst[s] = cc.kfreq * sqrt_mt / (sp * sqrt(sp));
         const double xx = sp / a.rchar;
-        double dd = -norm * pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
+        double dd = -norm * pow_ratio_planned(1.0 + xx, -a.go + a.gi, a.p_outer, xx, a.gi - 1.0, a.p_inner);
         dd += cc.c_dadt * mt3 * mr / (sp * sp * sp) / mr12;
         dadt[s] = dd;
     }
@@ -409,7 +421,9 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
         s_mt13 = pow(mt, 1.0 / 3.0);
     }
     __syncthreads();
-    const double mt3 = s_mt3, mr12 = s_mr12, mt13 = s_mt13;
+    const double mt13 = s_mt13;
+    const double gw_k = cc.c_dadt * s_mt3 * mr / s_mr12;   // GW rate = gw_k / sepa^3
+    const double inv_rchar = 1.0 / a.rchar;
     const long nzf = (long)a.n_redz * NF;
     const long base = (long)cell * nzf;
     for (long e = threadIdx.x; e < nzf; e += blockDim.x) {
@@ -422,13 +436,16 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
         double new_redz = zg[ni] + (new_time - ag[ni]) * sz[ni];
         double dcom = dg[ni] + (new_time - ag[ni]) * sd[ni];
         double target_frst_orb = ft[f] * (1.0 + new_redz);
-        const double cb = cbrt(target_frst_orb);   // target^(2/3) as cbrt(target)^2
-        double sp = cc.ksepa * mt13 / (cb * cb);
-        double xx = sp / a.rchar;
-        double dadt = -norm * pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
-        dadt += cc.c_dadt * mt3 * mr / (sp * sp * sp) / mr12;
+        // target^(-2/3) = r^2 with r = target^(-1/3): FP32 start and one FP64 Newton step,
+        // r (4 - y r^3) / 3 (relative error about 1e-14)
+        const double r0 = (double)rcbrtf((float)target_frst_orb);
+        const double r1 = r0 * (4.0 - target_frst_orb * (r0 * r0 * r0)) * (1.0 / 3.0);
+        double sp = cc.ksepa * mt13 * (r1 * r1);
+        double xx = sp * inv_rchar;
+        double dadt = -norm * pow_ratio_planned(1.0 + xx, -a.go + a.gi, a.p_outer, xx, a.gi - 1.0, a.p_inner);
+        dadt += gw_k / (sp * sp * sp);
         double tres = -(2.0 / 3.0) * sp / dadt;
-        double dcm = dcom / HGB_CY_MPC;
+        double dcm = dcom * (1.0 / HGB_CY_MPC);
         double cosmo_fact = cc.fourpi * (1.0 + new_redz) * (dcm * dcm);
         redz_final[base + e] = new_redz;
         diff_num[base + e] = nden[(long)cell * a.n_redz + kk] * tres * cosmo_fact;
@@ -532,7 +549,7 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
         if (valid && s <= S) {
             const double x = pow(10.0, myc[s]);
             const double xx = x / a.rchar;
-            rr[k] = pow_planned(1.0 + xx, -a.go + a.gi, a.p_outer) / pow_planned(xx, a.gi - 1.0, a.p_inner);
+            rr[k] = pow_ratio_planned(1.0 + xx, -a.go + a.gi, a.p_outer, xx, a.gi - 1.0, a.p_inner);
             gw[k] = cc.c_dadt * mt3 * mr / (x * x * x) / mr12;
             sp[k] = x;
         }

@@ -42,6 +42,7 @@ struct StrainArgs {
     double gw_src_const;
     const double *dc_val, *dc_der;
     int dc_n;
+    double dc_h;   // 1 / dc_n
 };
 
 // gravwaves.py:694-724 rearranged: hs = K mc (2 mc fr)^(2/3) / dc with fr = fc (1 + zbar) is evaluated
@@ -70,13 +71,16 @@ __device__ __forceinline__ double cell_strain(const BinGeom &g, const double *rz
     double b1 = 0.5 * (a11 + a01);
     double zb = 0.5 * (b1 + b0);
     if (!(zb > 0.0)) return 0.0;   // +inf comoving distance: zero strain
-    double dc = hgb::comoving_distance(s.dc_val, s.dc_der, s.dc_n, zb);
+    double dc = hgb::comoving_distance_fast(s.dc_val, s.dc_der, s.dc_n, s.dc_h, zb);
     double zp1 = 1.0 + zb;
     // (1 + z)^(2/3) = (1 + z) r with r = (1 + z)^(-1/3): FP32 start, one Newton step for the inverse
-    // cube root, r (4 - y r^3) / 3, in FP64 (relative error about 1e-14; 1 + z lies in (1, 12))
+    // cube root, r (4 - y r^3) / 3, in FP64 (relative error about 1e-14; 1 + z lies in (1, 12));
+    // 1 / dc likewise, q (2 - dc q) from an FP32 reciprocal
     const double r0 = (double)rcbrtf((float)zp1);
     const double r1 = r0 * (4.0 - zp1 * (r0 * r0 * r0)) * (1.0 / 3.0);
-    double hs = amp_mq * amp_f * (zp1 * r1) / dc;
+    const double q0 = (double)__frcp_rn((float)dc);
+    const double q1 = q0 * (2.0 - dc * q0);
+    double hs = amp_mq * amp_f * (zp1 * r1) * q1;
     return (hs * hs) * fc_df;
 }
 
@@ -185,7 +189,7 @@ int hgb_param_grids(const double *mt_cent, int n_mtot, int n_mrat, int n_redz, c
     HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
     HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
     BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
-    StrainArgs s{0.0, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    StrainArgs s{0.0, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n, 1.0 / cosmo->dc_n};
     cudaStream_t st = (cudaStream_t)stream;
     if (scale_log2) {
         cudaError_t err = cudaMemsetAsync(scale_log2, 0x80, 4 * sizeof(int), st);   // very negative
@@ -206,7 +210,7 @@ int hgb_integrate_3dx1d(const double *log10_mtot, int n_mtot, const double *mrat
     HGB_CHECK_ARG(log10_mtot && mrat && redz && dln_freq && dnum && number);
     HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
     BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
-    StrainArgs s{0.0, nullptr, nullptr, 0};
+    StrainArgs s{0.0, nullptr, nullptr, 0, 0.0};
     unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
     k_cells<true, false><<<cells, 256, 0, (cudaStream_t)stream>>>(g, s, nullptr, log10_mtot, mrat, redz, nullptr,
                                                                   dln_freq, dnum, nullptr, number, nullptr, nullptr);
@@ -220,7 +224,7 @@ int hgb_char_strain_sq(const double *mtot, int n_mtot, const double *mrat, int n
     HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
     HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
     BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
-    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n, 1.0 / cosmo->dc_n};
     unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
     size_t smem = sizeof(double) * 2 * n_freq;
     HGB_CHECK_ARG(smem <= 48 * 1024);
@@ -239,7 +243,7 @@ int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mt
     HGB_CHECK_ARG(n_mtot >= 2 && n_mrat >= 2 && n_redz >= 2 && n_freq >= 1);
     HGB_CHECK_ARG(cosmo->dc_val && cosmo->dc_der && cosmo->dc_n >= 2);
     BinGeom g{n_mtot, n_mrat, n_redz, n_freq};
-    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n};
+    StrainArgs s{gw_src_const, cosmo->dc_val, cosmo->dc_der, cosmo->dc_n, 1.0 / cosmo->dc_n};
     unsigned cells = (unsigned)((n_mtot - 1) * (n_mrat - 1));
     size_t smem = sizeof(double) * 2 * n_freq;
     HGB_CHECK_ARG(smem <= 48 * 1024);
