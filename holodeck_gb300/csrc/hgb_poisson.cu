@@ -81,10 +81,11 @@ constexpr int MAX_ATTEMPTS = 64;
 constexpr int MAX_PTRS_ITERS = 2 * RPT + 64;   // attempts of one lane over its RPT realizations
 constexpr int MAX_INVERSION = 4096;
 constexpr int MAX_PREFIX_EXTRA = 1024;   // prefix events beyond L (Normal draws below 1)
-constexpr double TABLE_MAX = 11500.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 9
-constexpr int TMAX = 1536;               // table entries (>= 14 sqrt(TABLE_MAX) + 9 = 1510)
-constexpr int HALF_WORDS = TMAX + 1024;  // the largest table: TMAX cdf words + 2^11 u16 guide cells
+constexpr double TABLE_MAX = 47000.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 10
+constexpr int TMAX = 3072;               // table entries (>= 14 sqrt(TABLE_MAX) + 10 = 3046)
+constexpr int HALF_WORDS = 1536 + 1024;  // tables up to 1536 entries (2^11 u16 guide cells) fit a half
 constexpr int ARENA_WORDS = 2 * HALF_WORDS;   // the halves alternate between build and draw
+static_assert(TMAX + 2048 <= ARENA_WORDS, "the largest table (2^12 guide cells) fits the whole arena");
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
 constexpr unsigned GUIDE_PURE = 0x8000u, GUIDE_ONE = 0x4000u, GUIDE_M = 0x0FFFu;   // guide cell fields
 static_assert(TMAX - 1 <= (int)GUIDE_M, "table entries fit the guide's index field");

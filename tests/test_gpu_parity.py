@@ -235,8 +235,8 @@ def test_philox_poisson_statistics(built_lib):
     """Counts of the Philox sampler follow Poisson(lambda) across all sampler regimes."""
     from holodeck_gb300 import cyutils
     from scipy import stats
-    lams = np.array([1e-7, 0.03, 0.099, 0.1, 0.12, 0.16, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 1.15e4, 1.16e4, 6.0e4,
-                     9.1e4, 5.0e6])
+    lams = np.array([1e-7, 0.03, 0.099, 0.1, 0.12, 0.16, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 1.15e4, 1.16e4, 4.69e4,
+                     4.71e4, 6.0e4, 9.1e4, 5.0e6])
     nreals = 20000
     # one bin per lambda, one frequency; L=0 so every source goes to the background sum
     number = lams.reshape(-1, 1, 1, 1)
