@@ -103,6 +103,18 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def issue_roofline(instr, t_launch, clk, n_sm=152, schedulers=4):
+    """Warp-instruction issue rate of a launch against the GPU's peak (one instruction per clock per
+    SM sub-partition at the sampled maximum SM clock)."""
+    mhz = (clk or {}).get("sm_max_mhz") or 2070.0
+    if not instr or not t_launch:
+        return None
+    peak = n_sm * schedulers * mhz * 1e6
+    achieved = instr / t_launch
+    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "instructions_per_launch": instr, "sm_mhz_for_peak": mhz}
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -206,9 +218,12 @@ def run_gpu(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg_bytes / t_real / 1e9
     traffic = None
+    instr = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
-            traffic = json.load(fh).get("k_bulk_bytes_per_launch")
+            prof = json.load(fh)
+            traffic = prof.get("k_bulk_bytes_per_launch")
+            instr = prof.get("k_bulk_warp_instructions_per_launch")
     except (OSError, ValueError):
         pass
 
@@ -229,7 +244,10 @@ def run_gpu(args):
             "roofline": {"kernel": "k_bulk", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
                          "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
                          "launch_s": t_real, "draws_per_s": draws / t_real,
-                         "note": "issue-bound sampler: HBM fraction shown for the contract, see profiles/"},
+                         "issue": issue_roofline(instr, t_real, clk),
+                         "note": ("issue-bound sampler: the HBM fraction is shown for the contract; the "
+                                  "issue object is the bound that applies (warp instructions per launch "
+                                  "from ncu, see profiles/)")},
             "clocks": clk,
             "cpu_baseline": cpu,
         }

@@ -96,6 +96,8 @@ SIGNATURES = [
     ("hgb_add_scatter_to_masses", _i, [ctypes.POINTER(HgbScatterPlan), _p, _i, _p, _sz, _p, _p]),
     ("hgb_dbn_2pwl", _i, [_p, _i, _i, _d, _i, _p, _d, _d, _d, _p, _p, _i, _p, _i, _p, _i, _p,
                           ctypes.POINTER(HgbCosmo), _p, _p, _p]),
+    ("hgb_dbn_2pwl_phase", _i, [_p, _i, _i, _d, _i, _p, _d, _d, _d, _p, _p, _i, _p, _i, _p, _i, _p,
+                                ctypes.POINTER(HgbCosmo), _p, _p, _i, _p]),
     ("hgb_dbn_gw", _i, [_p, _i, _p, _p, _i, _p, _i, _i, _p, ctypes.POINTER(HgbCosmo), _p, _p, _p]),
     ("hgb_integrate_3dx1d", _i, [_p, _i, _p, _i, _p, _i, _p, _i, _p, _p, _p]),
     ("hgb_char_strain_sq", _i, [_p, _i, _p, _i, _i, _p, _i, _p, _d, ctypes.POINTER(HgbCosmo), _p, _p, _p]),
@@ -168,7 +170,7 @@ def check(rc, what):
 #: per 8 key bits); used to report the launch count of a timed region
 KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
-    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_gw": 1,
+    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
     "hgb_loudest_hc_and_par_from_sorted": 6,

@@ -736,43 +736,61 @@ int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const d
     return hgb::check_launch();
 }
 
-int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
-                 const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
-                 const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
-                 const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
-                 double *redz_final, double *diff_num, void *stream) {
-    HGB_CHECK_ARG(fobs_orb && hard_norm && nden && mtot && mrat && redz && gmt_time && cosmo);
-    HGB_CHECK_ARG(redz_final && diff_num);
+int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                       const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                       const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                       const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                       double *redz_final, double *diff_num, int phase, void *stream) {
+    HGB_CHECK_ARG(phase >= 1 && phase <= 3);
+    HGB_CHECK_ARG(fobs_orb && hard_norm && mtot && mrat && cosmo && redz_final && diff_num);
+    HGB_CHECK_ARG(!(phase & 1) || (redz && gmt_time));
+    HGB_CHECK_ARG(!(phase & 2) || nden);
     HGB_CHECK_ARG(n_freq > 0 && num_steps > 0 && n_mtot > 0 && n_mrat > 0 && n_redz > 0);
     HGB_CHECK_ARG(cosmo->grid_size >= 2 && cosmo->grid_z && cosmo->grid_age && cosmo->grid_dcom);
     HGB_CHECK_ARG(sepa_init > 0.0 && rchar > 0.0);
     Dbn2plArgs a{log10(sepa_init), rchar, gamma_inner, gamma_outer, num_steps, n_freq, fobs_sorted ? 1 : 0,
                  n_mtot, n_mrat, n_redz, cosmo->grid_size, pow_plan(-gamma_outer + gamma_inner),
                  pow_plan(gamma_inner - 1.0)};
-    size_t smem = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
-                                    2 * (size_t)num_steps);
-    HGB_CHECK_ARG(smem <= 200 * 1024);
-    if (smem > 48 * 1024) {
-        cudaError_t err = cudaFuncSetAttribute(k_dbn_2pwl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (err != cudaSuccess) {
-            hgb::set_cuda_error(err);
-            return HGB_ERR_CUDA;
-        }
-    }
-    int threads = ((n_redz + 31) / 32) * 32;
-    if (threads > 256) threads = 256;
     unsigned blocks = (unsigned)((long)n_mtot * n_mrat);
-    k_dbn_2pwl<<<blocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden, mtot,
-                                                                mrat, redz, gmt_time, cosmo->grid_z,
-                                                                cosmo->grid_age, cosmo->grid_dcom, redz_final,
-                                                                diff_num);
-    int rc = hgb::check_launch();
-    if (rc) return rc;
-    size_t smem2 = sizeof(double) * ((size_t)5 * cosmo->grid_size + n_freq);
-    k_dbn_2pwl_eval<<<blocks, 256, smem2, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden, mtot,
-                                                                  mrat, cosmo->grid_z, cosmo->grid_age,
-                                                                  cosmo->grid_dcom, redz_final, diff_num);
-    return hgb::check_launch();
+    if (phase & 1) {
+        size_t smem = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
+                                        2 * (size_t)num_steps);
+        HGB_CHECK_ARG(smem <= 200 * 1024);
+        if (smem > 48 * 1024) {
+            cudaError_t err = cudaFuncSetAttribute(k_dbn_2pwl, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+            if (err != cudaSuccess) {
+                hgb::set_cuda_error(err);
+                return HGB_ERR_CUDA;
+            }
+        }
+        int threads = ((n_redz + 31) / 32) * 32;
+        if (threads > 256) threads = 256;
+        k_dbn_2pwl<<<blocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden,
+                                                                    mtot, mrat, redz, gmt_time, cosmo->grid_z,
+                                                                    cosmo->grid_age, cosmo->grid_dcom, redz_final,
+                                                                    diff_num);
+        int rc = hgb::check_launch();
+        if (rc) return rc;
+    }
+    if (phase & 2) {
+        size_t smem2 = sizeof(double) * ((size_t)5 * cosmo->grid_size + n_freq);
+        k_dbn_2pwl_eval<<<blocks, 256, smem2, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden,
+                                                                      mtot, mrat, cosmo->grid_z, cosmo->grid_age,
+                                                                      cosmo->grid_dcom, redz_final, diff_num);
+        return hgb::check_launch();
+    }
+    return HGB_OK;
+}
+
+int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                 const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                 const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                 const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                 double *redz_final, double *diff_num, void *stream) {
+    return hgb_dbn_2pwl_phase(fobs_orb, n_freq, fobs_sorted, sepa_init, num_steps, hard_norm, rchar, gamma_inner,
+                              gamma_outer, nden, mtot, n_mtot, mrat, n_mrat, redz, n_redz, gmt_time, cosmo,
+                              redz_final, diff_num, 3, stream);
 }
 
 int hgb_dbn_gw(const double *fobs_orb, int n_freq, const double *nden, const double *mtot, int n_mtot,

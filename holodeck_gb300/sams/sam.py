@@ -26,6 +26,18 @@ GPF_USES_MTOT = False        #: sam.py:58
 GMT_USES_MTOT = False        #: sam.py:59
 
 
+_AUX_STREAMS = {}
+
+
+def _aux_stream(device):
+    """One second stream per device for grid stages that can overlap the current stream's work."""
+    t = D.torch()
+    key = t.device(device).index
+    if key not in _AUX_STREAMS:
+        _AUX_STREAMS[key] = t.cuda.Stream(device=device)
+    return _AUX_STREAMS[key]
+
+
 class Semi_Analytic_Model:
     """Semi-analytic model of MBH-binary populations on an (mtot, mrat, redz) grid (sam.py:66-234)."""
 
@@ -120,6 +132,12 @@ class Semi_Analytic_Model:
         """Device (density, gmt_time or None, redz_prime or None), computed once per instance."""
         if self._density_t is not None:
             return self._density_t, self._gmt_time_t, self._redz_prime_t
+        dens, gmt_time, redz_prime = self._static_density_launch()
+        self._scatter_finish(dens, gmt_time, redz_prime)
+        return dens, gmt_time, redz_prime
+
+    def _static_density_launch(self):
+        """The static density before the M-Mbulge scatter, with gmt_time and redz_prime."""
         import ctypes
         t = D.torch()
         mt, mr, rz = self._edges_device()
@@ -134,6 +152,10 @@ class Semi_Analytic_Model:
         st = D.StatusWord(dev)
         N.call("hgb_static_density", ctypes.byref(model), dc.ref, N.ptr(mt), mt.numel(), N.ptr(mr), mr.numel(),
                N.ptr(rz), rz.numel(), N.ptr(dens), N.ptr(gmt_time), N.ptr(redz_prime), st.ptr, N.stream_handle())
+        return dens, gmt_time, redz_prime
+
+    def _scatter_finish(self, dens, gmt_time, redz_prime):
+        """Scatter and stalled-bin zeroing in place; caches the final density on the instance."""
         scatter = self._mmbulge._scatter_dex
         if scatter > 0.0:
             from . import scatter as _scatter
@@ -141,7 +163,7 @@ class Semi_Analytic_Model:
         if redz_prime is not None:
             N.call("hgb_zero_stalled", N.ptr(dens), N.ptr(redz_prime), int(dens.numel()), N.stream_handle())
         self._density_t, self._gmt_time_t, self._redz_prime_t = dens, gmt_time, redz_prime
-        return dens, gmt_time, redz_prime
+        return dens
 
     @property
     def static_binary_density(self):
@@ -181,6 +203,32 @@ class Semi_Analytic_Model:
             return sam_cyutils.dbn_gw_device(fobs_orb, dens, mt, mr, redz_prime, cosmo=cosmo)
         raise ValueError(f"Unexpected `hard` value {hard}!")
 
+    def _dbn_2pwl_overlapped(self, hard, fobs_orb):
+        """_dbn_device for Fixed_Time_2PL_SAM on a fresh instance, with the separation-step walk (which
+        needs gmt_time but not the density) on a second stream while the current stream applies the
+        M-Mbulge scatter; the evaluation, which needs the final density, follows on the current
+        stream.  Same results as _dbn_device."""
+        t = D.torch()
+        dens, gmt_time, redz_prime = self._static_density_launch()
+        mt, mr, rz = self._edges_device()
+        main = t.cuda.current_stream()
+        side = _aux_stream(main.device)
+        static_done = t.cuda.Event()
+        static_done.record(main)
+        side.wait_event(static_done)
+        with t.cuda.stream(side):
+            redz_final, diff_num = sam_cyutils.dbn_2pwl_device(fobs_orb, hard, None, mt, mr, rz, gmt_time,
+                                                               cosmo=self._cosmo, phase=1)
+            walk_done = t.cuda.Event()
+            walk_done.record(side)
+        gmt_time.record_stream(side)
+        self._scatter_finish(dens, gmt_time, redz_prime)
+        main.wait_event(walk_done)
+        redz_final.record_stream(main)
+        diff_num.record_stream(main)
+        return sam_cyutils.dbn_2pwl_device(fobs_orb, hard, dens, mt, mr, rz, gmt_time, cosmo=self._cosmo, phase=2,
+                                           out=(redz_final, diff_num))
+
     def dynamic_binary_number_at_fobs(self, hard, fobs_orb, use_cython=True, **kwargs):
         """(grid, dnum, redz_final) like sam.py:400-466 (``use_cython`` is accepted and ignored)."""
         redz_final, dnum = self._dbn_device(hard, fobs_orb)
@@ -202,7 +250,11 @@ class Semi_Analytic_Model:
         fobs_gw_cents = utils.midpoints(fobs_gw_edges)
         fobs_orb_edges = fobs_gw_edges / 2.0
         fobs_orb_cents = fobs_gw_cents / 2.0
-        redz_final, diff_num = self._dbn_device(hard, fobs_orb_cents)
+        if (self._density_t is None and self._gmt is not None and isinstance(hard, hardening.Fixed_Time_2PL_SAM)
+                and self._mmbulge._scatter_dex > 0.0):
+            redz_final, diff_num = self._dbn_2pwl_overlapped(hard, fobs_orb_cents)
+        else:
+            redz_final, diff_num = self._dbn_device(hard, fobs_orb_cents)
         number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final)
         if params:
             edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]

@@ -43,8 +43,13 @@ def dynamic_binary_number_at_fobs(fobs_orb, sam, hard, cosmo=None):
     return _out(redz_final, like_torch), _out(diff_num, like_torch)
 
 
-def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None):
-    """Device arrays in, device (redz_final, diff_num) out (sam_cyutils.pyx:510-781)."""
+def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None, phase=3, out=None):
+    """Device arrays in, device (redz_final, diff_num) out (sam_cyutils.pyx:510-781).
+
+    ``phase`` 1 runs only the separation-step walk (``dens`` may be None; the outputs then hold the
+    bracketing step and time, see hgb_dbn_2pwl_phase), 2 only the evaluation into ``out`` from
+    phase 1, 3 both.
+    """
     t = D.torch()
     cosmo = _cosmo if cosmo is None else cosmo
     dc = D.device_cosmology(cosmo)
@@ -55,14 +60,17 @@ def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None
     else:   # host input: decide on the host, no device round trip
         fh = np.asarray(fobs_orb, dtype=np.float64).ravel()
         sorted_ok = int(bool(np.all(fh[1:] >= fh[:-1])))
-    shape = tuple(dens.shape) + (nf,)
-    redz_final = t.empty(shape, dtype=t.float64, device=dens.device)
-    diff_num = t.empty(shape, dtype=t.float64, device=dens.device)
+    if out is None:
+        grid = (int(mtot.numel()), int(mrat.numel()), int(redz.numel()))
+        redz_final = t.empty(grid + (nf,), dtype=t.float64, device=mtot.device)
+        diff_num = t.empty(grid + (nf,), dtype=t.float64, device=mtot.device)
+    else:
+        redz_final, diff_num = out
     norm = D.as_device(hard._norm_device())
-    N.call("hgb_dbn_2pwl", N.ptr(fo), nf, sorted_ok, float(hard._sepa_init), int(hard._num_steps), N.ptr(norm),
-           float(hard._rchar), float(hard._gamma_inner), float(hard._gamma_outer), N.ptr(dens), N.ptr(mtot),
-           int(mtot.numel()), N.ptr(mrat), int(mrat.numel()), N.ptr(redz), int(redz.numel()), N.ptr(gmt_time),
-           dc.ref, N.ptr(redz_final), N.ptr(diff_num), N.stream_handle())
+    N.call("hgb_dbn_2pwl_phase", N.ptr(fo), nf, sorted_ok, float(hard._sepa_init), int(hard._num_steps),
+           N.ptr(norm), float(hard._rchar), float(hard._gamma_inner), float(hard._gamma_outer), N.ptr(dens),
+           N.ptr(mtot), int(mtot.numel()), N.ptr(mrat), int(mrat.numel()), N.ptr(redz), int(redz.numel()),
+           N.ptr(gmt_time), dc.ref, N.ptr(redz_final), N.ptr(diff_num), int(phase), N.stream_handle())
     return redz_final, diff_num
 
 

@@ -206,6 +206,16 @@ int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sep
                  const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
                  double *redz_final, double *diff_num, void *stream);
 
+/* hgb_dbn_2pwl in two phases, so that the first can overlap the M-Mbulge scatter: phase 1 walks the
+ * separation steps (needs gmt_time, not the density; nden may be NULL) and leaves, per element, the
+ * bracketing step index in redz_final and the target's time in diff_num; phase 2 turns them into
+ * redz_final / diff_num with the final density nden.  phase 3 is both (= hgb_dbn_2pwl). */
+int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                       const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                       const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                       const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                       double *redz_final, double *diff_num, int phase, void *stream);
+
 /* Same for Hard_GW (GW-only) hardening.  Replaces _dynamic_binary_number_at_fobs_gw,
  * sam_cyutils.pyx:788-899.  redz_prime is (M, Q, Z). */
 int hgb_dbn_gw(const double *fobs_orb, int n_freq, const double *nden, const double *mtot, int n_mtot,

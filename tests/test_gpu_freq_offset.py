@@ -47,3 +47,31 @@ def test_frequency_chunks_match_one_call(built_lib):
     assert np.array_equal(ss, ss1)
     assert np.all(np.abs(bg - bg1) <= 1e-5 * np.abs(bg1))
     assert np.all(bg > 0)
+
+
+@pytest.mark.gpu
+def test_overlapped_dbn_matches_sequential(built_lib):
+    """gwb() on a fresh model walks the separation steps on a second stream while the scatter runs;
+    the results equal the sequential stages bit for bit."""
+    import torch
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    from holodeck_gb300 import single_sources
+
+    def model():
+        sam = H.sams.Semi_Analytic_Model(shape=(16, 15, 14), gpf=H.sams.GPF_Power_Law(), gmt=H.sams.GMT_Power_Law(),
+                                         mmbulge=H.host_relations.MMBulge_KH2013(scatter_dex=0.3))
+        hard = H.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * C.GYR, rchar=100.0 * C.PC, gamma_inner=-1.0,
+                                              gamma_outer=2.5)
+        return sam, hard
+
+    _, fe = H.utils.pta_freqs(16.0 * C.YR, 6)
+    R, L, seed = 64, 2, 99
+    sam, hard = model()
+    ss, bg = sam.gwb(fe, hard=hard, realize=R, loudest=L, seed=seed, return_torch=True)
+    sam2, hard2 = model()
+    rf, dn = sam2._dbn_device(hard2, H.utils.midpoints(fe) / 2.0)
+    number, h2fdf = sam2._number_and_strain(fe / 2.0, dn, rf)
+    ss2, bg2 = single_sources.ss_realize_device(number, h2fdf, R, L, seed=seed)
+    torch.cuda.synchronize()
+    assert torch.equal(ss, ss2) and torch.equal(bg, bg2)
