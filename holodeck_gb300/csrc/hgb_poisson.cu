@@ -703,6 +703,7 @@ struct BulkArgs {
     int nchunk;        // chunk c holds tiles c, c + nchunk, c + 2 nchunk, ...
     uint32_t domain;
     PhiloxKey key;
+    int *wide_flag;    // set by k_bulk when it leaves bins to k_bulk_wide (zeroed before the launch)
 };
 
 // Inversion table of one table-kind bin (lambda in [10, TABLE_MAX]), built by a warp or a block:
@@ -1224,16 +1225,23 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
         } else if (n_sparse > 0) {
             // The block's realizations cut into runs of 2^lg per bin (about one expected event per
             // run); the runs of the tile's sparse bins are numbered in list order and shared out
-            // over the threads, each walking its run by geometric gaps.  Events go to per-tile FP32
-            // sums by realization in the arena (atomics; a few events per realization and tile),
-            // which each thread then folds into its Kahan sums.
-            float *sub = reinterpret_cast<float *>(s.u.arena);   // [RPT * RB], realization r at sub[r]
+            // over the threads, each walking its run by geometric gaps.  Events go to per-tile sums
+            // by realization in the arena, in 64-bit fixed point with unit 2^(e - 50) for e the
+            // largest exponent of the tile's sparse strains: integer atomics, so the sums do not
+            // depend on the order the threads reach them (4096 times the largest term of headroom;
+            // a realization sees a few events per tile).  Each thread then folds its slots into its
+            // Kahan sums.
+            unsigned long long *sub = reinterpret_cast<unsigned long long *>(s.u.arena);   // [RPT * RB]
             const int nr_blk = min(RB * RPT, a.nr - (int)blockIdx.z * RB * RPT);
-            int runs = 0;
+            int runs = 0, e_hs = -1000;
             if (t < n_sparse) {
-                const int lg = s.sp_lg[s.list[KIND_SPARSE][t]];
+                const int js = s.list[KIND_SPARSE][t];
+                const int lg = s.sp_lg[js];
                 runs = (nr_blk + (1 << lg) - 1) >> lg;
+                frexpf(s.hs[js], &e_hs);
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) e_hs = max(e_hs, __shfl_xor_sync(0xffffffffu, e_hs, o));
             int incl = runs;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -1241,17 +1249,20 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
                 if (lane >= o) incl += y;
             }
             __syncthreads();   // the arena and the scan words are free
-            if (lane == 31) s.scan[warp] = (unsigned long long)incl;
+            if (lane == 31) s.scan[warp] = ((unsigned long long)(unsigned)(e_hs + 2048) << 32) | (unsigned)incl;
 #pragma unroll
-            for (int i = 0; i < RPT; i++) sub[i * RB + t] = 0.0f;
+            for (int i = 0; i < RPT; i++) sub[i * RB + t] = 0ull;
             __syncthreads();
-            int before = 0, total = 0;
+            int before = 0, total = 0, e_max = -1000;
 #pragma unroll
             for (int w = 0; w < NWARP; w++) {
-                const int v = (int)s.scan[w];
+                const unsigned long long x = s.scan[w];
+                const int v = (int)(unsigned)x;
                 before += (w < warp) ? v : 0;
                 total += v;
+                e_max = max(e_max, (int)(x >> 32) - 2048);
             }
+            const int fx_shift = 50 - e_max;   // term x -> round(x 2^fx_shift)
             if (t < n_sparse) s.sp_start[t] = before + incl - runs;
             __syncthreads();
             const int *q_blk = SORTED ? q_row - t : nullptr;   // first bulk positions of the block's realizations
@@ -1282,18 +1293,20 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
                     if (gap >= (float)(re - r)) break;
                     r += (int)gap;
                     const int n = truncated_count_f32(lf, u24(w.z), d_status);
-                    if (!check || pos >= __ldg(q_blk + r)) atomicAdd(&sub[r], (float)n * hs);
+                    if (!check || pos >= __ldg(q_blk + r))
+                        atomicAdd(&sub[r], __float2ull_rn(ldexpf((float)n * hs, fx_shift)));
                     if (++r >= re) break;
                 }
             }
             __syncthreads();
 #pragma unroll
             for (int i = 0; i < RPT; i++)
-                if (i < rpt) kahan_add(acc_r[i], comp_r[i], sub[i * RB + t]);
+                if (i < rpt) kahan_add(acc_r[i], comp_r[i], (float)ldexp((double)sub[i * RB + t], -fx_shift));
         }
 
         // ---- PTRS64 / Normal (real-valued counts, cyutils.pyx:1327-1330 / :887-891); without the
         // parameter sums these bins go to k_bulk_wide, which keeps their FP64 code out of this kernel
+        if (!PARAMS && t == 0 && kind_count(s, KIND_WIDE) > 0) atomicOr(a.wide_flag, 1);
         const int n_wide = PARAMS ? kind_count(s, KIND_WIDE) : 0;
 #pragma unroll 1
         for (int li = 0; li < n_wide; li++) {
@@ -1341,6 +1354,7 @@ __global__ void __launch_bounds__(RB) k_bulk_wide(BulkArgs a, const double *__re
     __shared__ double w_lam[RB], w_h[RB];
     __shared__ int w_pos[RB];
     __shared__ int w_count[NWARP];
+    if (*(volatile int *)a.wide_flag == 0) return;   // k_bulk met no such bin (uniform over the grid)
     const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
     const int r0 = blockIdx.z * RB * RPT + t;
@@ -1520,7 +1534,7 @@ int choose_nchunk(long nb, int nf, int nr) {
 }
 
 struct LoudLayout {
-    size_t off_lam, off_h, off_cum, off_seg, off_q, off_bgp, off_part, total;
+    size_t off_lam, off_h, off_cum, off_seg, off_q, off_bgp, off_part, off_flag, total;
     int nchunk;
 };
 
@@ -1544,6 +1558,8 @@ LoudLayout loud_layout(long nb, int nf, int nr, int mode) {
         o += align256(sizeof(double) * nfr);
         L.off_part = o;
         o += align256(sizeof(double) * (size_t)L.nchunk * nfr);
+        L.off_flag = o;
+        o += 256;
     }
     L.total = o;
     return L;
@@ -1558,6 +1574,7 @@ BulkArgs bulk_args(long nb, int nf, int nr, int nchunk, uint64_t seed, uint32_t 
     a.nchunk = nchunk;
     a.domain = domain;
     a.key = make_key(seed);
+    a.wide_flag = nullptr;
     return a;
 }
 
@@ -1666,6 +1683,8 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
                                                                             q, d_status);
     if ((rc = hgb::check_launch())) return rc;
     BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u, freq_offset);
+    a.wide_flag = (int *)(w + L.off_flag);
+    cudaMemsetAsync(a.wide_flag, 0, sizeof(int), st);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
     if ((rc = bulk_event(0, st))) return rc;
     k_bulk<true, false><<<grid, RB, 0, st>>>(a, ParArgs{}, lam_s, h_s, q, part, d_status);
@@ -1755,6 +1774,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
                                                                            d_status);
     if ((rc = hgb::check_launch())) return rc;
     BulkArgs a = bulk_args(n_bins, n_freq, nreals, L.nchunk, seed, 0u);
+    a.wide_flag = (int *)(w + L.off_flag);   // unused: the parameter kernel draws its wide bins itself
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
     cudaError_t err = cudaFuncSetAttribute(k_bulk<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)PAR_SMEM);
@@ -1771,7 +1791,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
 size_t hgb_sam_poisson_gwb_workspace_bytes(long n_bins, int n_freq, int nreals) {
     if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
     long nchunk = choose_nchunk(n_bins, n_freq, nreals);
-    return align256(sizeof(double) * (size_t)nchunk * n_freq * nreals);
+    return align256(sizeof(double) * (size_t)nchunk * n_freq * nreals) + 256;   // partials, wide-bin flag
 }
 
 int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, int n_freq, int nreals, int mode,
@@ -1795,6 +1815,8 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     if (!workspace || workspace_bytes < hgb_sam_poisson_gwb_workspace_bytes(n_bins, n_freq, nreals))
         return HGB_ERR_WORKSPACE;
     BulkArgs a = bulk_args(n_bins, n_freq, nreals, choose_nchunk(n_bins, n_freq, nreals), seed, DOMAIN_GWB);
+    a.wide_flag = (int *)((char *)workspace + align256(sizeof(double) * (size_t)a.nchunk * n_freq * nreals));
+    cudaMemsetAsync(a.wide_flag, 0, sizeof(int), st);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));
     k_bulk<false, false><<<grid, RB, 0, st>>>(a, ParArgs{}, number, hc2, nullptr, (double *)workspace, d_status);
     int rc = hgb::check_launch();
