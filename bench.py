@@ -8,8 +8,13 @@ gamma_inner=-1, gamma_outer=+2.5, sepa_init=1 kpc); 40 harmonics of 1/(16 yr); 1
 find the hardening normalisation, and gwb() (dynamic binary number, integration, strain, sort,
 Poisson realizations with the loudest split).  value = realizations / s.
 
+The line also carries ``batched``: a whole library of 512 Latin-hypercube samples of
+PS_Classic_Phenom_Uniform, each on its own grid (40-91 per axis) with its own realization count
+(100-1000), run through the batched library API (realizations/s over the library).
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
     python bench.py --stages        # per-stage device times
+    python bench.py --batched       # only the batched-library measurement
     python bench.py --profile --nfreqs K   # one untimed evaluation (the program ncu captures)
 
 --impl reference times the CPU restatement of the reference path (the oracle) on the host cores.
@@ -206,7 +211,8 @@ def run_gpu(args):
     # strain of the bins with a nonzero expectation (8 B each), each realization's first bulk
     # position read, the per-chunk partials written
     n_rgroups = -(-NREALS // 1024)
-    nchunk = max(1, -(-152 * 6 * 2 // (NFREQ * n_rgroups)))
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    nchunk = max(1, -(-n_sm * 6 * lib.hgb_get_bulk_waves() // (NFREQ * n_rgroups)))
     n_pos = int((number > 0).sum().item())
     alg_bytes = (8 * nb * NFREQ + 8 * n_pos) * n_rgroups + 4 * NFREQ * NREALS + 8 * nchunk * NFREQ * NREALS
     peaks = {}
@@ -227,6 +233,7 @@ def run_gpu(args):
     except (OSError, ValueError):
         pass
 
+    batched = run_batched(args, rank, world) if args.batched_samples > 0 else None
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
     if rank == 0:
         line = {
@@ -250,10 +257,51 @@ def run_gpu(args):
                                   "from ncu, see profiles/)")},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+BATCH_CONFIG = ("batched library: Latin-hypercube samples (seed 0) of PS_Classic_Phenom_Uniform (gsmf_phi0, "
+                "gsmf_mchar0_log10, mmb_mamp_log10, mmb_scatter_dex, hard_time, hard_gamma_inner), per-sample grid "
+                "uniform integers in [40, 91] per axis and realizations in [100, 1000] (default_rng(0)), "
+                "40 frequencies, 10 loudest")
+
+
+def run_batched(args, rank=0, world=1):
+    """The batched-library workload through the public library API (host parameters in, host arrays
+    out): samples rank, rank + world, ... of the library on this rank's GPU.  Returns the object the
+    bench line carries (on rank 0; the wall time is the max over ranks)."""
+    import torch
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
+    n = args.batched_samples
+    space = PS_Classic_Phenom_Uniform(nsamples=n, seed=0)
+    shapes, nreals = batch.random_shapes(n, seed=0)
+    stats = {}
+    out = batch.run_library(space, shapes, nreals, nfreqs=NFREQ, nloudest=NLOUD, seed=1,
+                            indices=list(range(rank, n, world)), stats=stats)
+    wall, reals, draws = stats["seconds"], stats["realizations"], stats["draws"]
+    if world > 1:
+        import torch.distributed as dist
+        mx = torch.tensor([wall], dtype=torch.float64, device="cuda")
+        tt = torch.tensor([reals, draws], dtype=torch.float64, device="cuda")
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
+        wall, reals, draws = float(mx.item()), float(tt[0].item()), float(tt[1].item())
+    d2h = sum(sum(v.nbytes for k, v in r.items() if isinstance(v, np.ndarray)) for r in out if r is not None)
+    tuning = stats.get("tuning") or {}
+    table = tuning.get("table", {})
+    one = table.get(f"1,{stats['waves']}")
+    best = table.get(f"{stats['workers']},{stats['waves']}")
+    return {"workload": BATCH_CONFIG, "samples": n, "failed": stats["failed"], "seconds": wall,
+            "value": reals / wall, "unit": UNIT, "samples_per_s": n / wall, "draws_per_s": draws / wall,
+            "realizations": int(reals), "schedule": {"workers": stats["workers"], "waves": stats["waves"]},
+            "autotune_draws_per_s": table,
+            "speedup_vs_one_worker_in_probe": (best / one) if (best and one) else None,
+            "e2e": "host parameters in, host hc_ss / hc_bg out; per-sample scatter plans built on the host "
+                   "inside the timed region", "d2h_bytes": int(d2h)}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -421,8 +469,15 @@ def main():
     ap.add_argument("--profile", action="store_true", help="run warmup + 1 untimed evaluations (for ncu)")
     ap.add_argument("--nfreqs", type=int, default=NFREQ, help="frequencies of a --profile run")
     ap.add_argument("--stages", action="store_true", help="per-stage device times of one model evaluation")
+    ap.add_argument("--batched-samples", type=int, default=512,
+                    help="library samples of the batched measurement carried by the bench line (0: skip)")
+    ap.add_argument("--batched", action="store_true", help="only the batched-library measurement")
     args = ap.parse_args()
-    if args.profile:
+    if args.batched and args.impl != "reference":
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps({"metric": METRIC, "batched": run_batched(args)}))
+    elif args.profile:
         run_profile(args)
     elif args.stages:
         run_stages(args)

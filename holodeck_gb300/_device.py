@@ -124,6 +124,22 @@ def device_cosmology(cosmo, dev=None):
     return hit
 
 
+_SIDE_STREAMS = {}
+
+
+def side_stream(role, dev=None):
+    """A second stream for grid stages that overlap the calling thread's current stream: one per
+    (device, current stream, role), so host workers that each run on their own stream never share
+    one."""
+    t = torch()
+    cur = t.cuda.current_stream(device(dev))
+    key = (cur.device.index, cur.cuda_stream, role)
+    s = _SIDE_STREAMS.get(key)
+    if s is None:
+        s = _SIDE_STREAMS.setdefault(key, t.cuda.Stream(device=cur.device))
+    return s
+
+
 def workspace(nbytes, dev=None):
     """A byte buffer for an entry point's scratch memory (from torch's caching allocator)."""
     t = torch()

@@ -6,6 +6,7 @@ loaded, or no CUDA device is present, calls raise :class:`NativeUnavailable`.
 
 import ctypes
 import os
+import threading
 
 import numpy as np
 
@@ -117,6 +118,8 @@ SIGNATURES = [
     ("hgb_model_details", _i, [_p, _p, _p, _p, _i, _i, _i, _i] + [_p] * 12),
     ("hgb_bulk_timing", _i, [_i]),
     ("hgb_bulk_last_ms", ctypes.c_float, []),
+    ("hgb_set_bulk_waves", _i, [_i]),
+    ("hgb_get_bulk_waves", _i, []),
     ("hgb_sam_poisson_gwb_workspace_bytes", _sz, [_l, _i, _i]),
     ("hgb_sam_poisson_gwb", _i, [_p, _p, _l, _i, _i, _i, _u64, _p, _p, _p, _sz, _p, _p]),
 ]
@@ -176,6 +179,7 @@ KERNELS_PER_CALL = {
     "hgb_loudest_hc_and_par_from_sorted": 6,
 }
 _launches = [0]
+_launch_lock = threading.Lock()
 
 
 def reset_launch_count():
@@ -190,7 +194,8 @@ def call(name, *args):
     """Call an entry point and raise on a non-zero return code."""
     fn = getattr(load(), name)
     check(fn(*args), name)
-    _launches[0] += KERNELS_PER_CALL.get(name, 0)
+    with _launch_lock:
+        _launches[0] += KERNELS_PER_CALL.get(name, 0)
 
 
 def ptr(t):

@@ -114,6 +114,9 @@ __device__ __forceinline__ double comoving_distance_fast(const double *dval, con
 
 __host__ __device__ __forceinline__ long ceil_div(long a, long b) { return (a + b - 1) / b; }
 
+// Multiprocessor count of the current device (queried once per device, 152 on a GB300).
+int sm_count();
+
 }  // namespace hgb
 
 #define HGB_CHECK_ARG(cond)                        \

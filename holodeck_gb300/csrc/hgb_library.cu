@@ -2,6 +2,8 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "hgb_common.cuh"
 
 namespace {
@@ -29,6 +31,17 @@ int check_launch() {
         return HGB_ERR_CUDA;
     }
     return HGB_OK;
+}
+
+int sm_count() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
 }
 
 CyConst cy_const() {

@@ -64,6 +64,8 @@
 
 #include <type_traits>
 
+#include <atomic>
+
 #include "hgb_common.cuh"
 
 namespace {
@@ -1522,9 +1524,16 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
-int choose_nchunk(long nb, int nf, int nr) {
+// Waves of resident k_bulk blocks (six per SM) that the chunk count aims for; set by hgb_set_bulk_waves.
+// Workspace sizes are always computed for HGB_BULK_WAVES_MAX, so a change between a workspace query
+// and a launch only leaves part of the workspace unused.
+std::atomic<int> g_bulk_waves{2};
+
+int bulk_waves() { return g_bulk_waves.load(std::memory_order_relaxed); }
+
+int choose_nchunk(long nb, int nf, int nr, int waves) {
     long blocks = (long)n_rgroups(nr) * nf;
-    long target = 152L * 6 * 2;   // two waves of resident blocks (six per SM) on 152 SMs
+    long target = (long)hgb::sm_count() * 6 * waves;
     long nchunk = hgb::ceil_div(target, blocks);
     long maxc = hgb::ceil_div(nb, 8L * RB);
     if (nchunk > maxc) nchunk = maxc;
@@ -1538,9 +1547,9 @@ struct LoudLayout {
     int nchunk;
 };
 
-LoudLayout loud_layout(long nb, int nf, int nr, int mode) {
+LoudLayout loud_layout(long nb, int nf, int nr, int mode, int waves) {
     LoudLayout L{};
-    L.nchunk = choose_nchunk(nb, nf, nr);
+    L.nchunk = choose_nchunk(nb, nf, nr, waves);
     const long nfr = (long)nf * nr;
     size_t o = 0;
     L.off_lam = o;
@@ -1623,7 +1632,7 @@ float hgb_bulk_last_ms(void) {
 size_t hgb_loudest_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode) {
     (void)nloud;
     if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
-    return loud_layout(n_bins, n_freq, nreals, mode).total;
+    return loud_layout(n_bins, n_freq, nreals, mode, HGB_BULK_WAVES_MAX).total;
 }
 
 int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n_bins, int n_freq, int nreals,
@@ -1652,8 +1661,9 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
         cudaMemsetAsync(hc2bg, 0, sizeof(double) * (size_t)n_freq * nreals, st);
         return hgb::check_launch();
     }
-    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
-    if (!workspace || workspace_bytes < L.total) return HGB_ERR_WORKSPACE;
+    if (!workspace || workspace_bytes < hgb_loudest_workspace_bytes(n_bins, n_freq, nreals, nloud, mode))
+        return HGB_ERR_WORKSPACE;
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode, bulk_waves());
     char *w = (char *)workspace;
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
@@ -1699,7 +1709,7 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
 size_t hgb_loudest_par_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode) {
     (void)nloud;
     if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
-    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode, HGB_BULK_WAVES_MAX);
     size_t o = L.total;
     if (mode == HGB_RNG_PHILOX) {
         const size_t nfr = (size_t)n_freq * nreals;
@@ -1729,7 +1739,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     const size_t need = hgb_loudest_par_workspace_bytes(n_bins, n_freq, nreals, nloud, mode);
     if (!workspace || workspace_bytes < need) return HGB_ERR_WORKSPACE;
     cudaStream_t st = (cudaStream_t)stream;
-    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode);
+    LoudLayout L = loud_layout(n_bins, n_freq, nreals, mode, bulk_waves());
     char *w = (char *)workspace;
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
@@ -1788,9 +1798,17 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     return hgb::check_launch();
 }
 
+int hgb_set_bulk_waves(int waves) {
+    HGB_CHECK_ARG(waves >= 1 && waves <= HGB_BULK_WAVES_MAX);
+    g_bulk_waves.store(waves, std::memory_order_relaxed);
+    return HGB_OK;
+}
+
+int hgb_get_bulk_waves(void) { return bulk_waves(); }
+
 size_t hgb_sam_poisson_gwb_workspace_bytes(long n_bins, int n_freq, int nreals) {
     if (n_bins <= 0 || n_freq <= 0 || nreals <= 0) return 0;
-    long nchunk = choose_nchunk(n_bins, n_freq, nreals);
+    long nchunk = choose_nchunk(n_bins, n_freq, nreals, HGB_BULK_WAVES_MAX);
     return align256(sizeof(double) * (size_t)nchunk * n_freq * nreals) + 256;   // partials, wide-bin flag
 }
 
@@ -1814,7 +1832,8 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     }
     if (!workspace || workspace_bytes < hgb_sam_poisson_gwb_workspace_bytes(n_bins, n_freq, nreals))
         return HGB_ERR_WORKSPACE;
-    BulkArgs a = bulk_args(n_bins, n_freq, nreals, choose_nchunk(n_bins, n_freq, nreals), seed, DOMAIN_GWB);
+    BulkArgs a = bulk_args(n_bins, n_freq, nreals, choose_nchunk(n_bins, n_freq, nreals, bulk_waves()), seed,
+                          DOMAIN_GWB);
     a.wide_flag = (int *)((char *)workspace + align256(sizeof(double) * (size_t)a.nchunk * n_freq * nreals));
     cudaMemsetAsync(a.wide_flag, 0, sizeof(int), st);
     dim3 grid((unsigned)a.nchunk, (unsigned)n_freq, (unsigned)n_rgroups(nreals));

@@ -20,17 +20,6 @@ class Hard_GW(_Hardening):
         return False
 
 
-_SIDE_STREAMS = {}
-
-
-def _side_stream(dev):
-    t = D.torch()
-    key = str(dev)
-    if key not in _SIDE_STREAMS:
-        _SIDE_STREAMS[key] = t.cuda.Stream(device=dev)
-    return _SIDE_STREAMS[key]
-
-
 class Fixed_Time_2PL_SAM(_Hardening):
     """Two-power-law hardening normalised to a fixed total lifetime (hardening.py:1371-1457).
 
@@ -52,7 +41,7 @@ class Fixed_Time_2PL_SAM(_Hardening):
         # The root finding depends only on the mass grid: it runs on a side stream, concurrently with the
         # density and scatter stages that the next gwb() call enqueues, and the dbn stage waits on it.
         main = t.cuda.current_stream(mt_d.device)
-        side = _side_stream(mt_d.device)
+        side = D.side_stream("hardening_norm", mt_d.device)
         side.wait_stream(main)
         with t.cuda.stream(side):
             mtot, mrat = t.meshgrid(mt_d, mr_d, indexing="ij")

@@ -1,0 +1,237 @@
+"""Batched library runs on one GPU.
+
+A library is many independent model evaluations: the samples of a parameter space, each on its own
+(mtot, mrat, redz) grid shape and with its own realization count (the per-sample work of
+librarian/gen_lib.py:run_sam_at_pspace_num, which the reference spreads over MPI ranks).  Here one
+process drives one GPU with a pool of host workers.  Each worker owns a CUDA stream (and the side
+streams paired with it) and runs whole samples through :func:`lib_tools.run_model`, so the
+latency-bound FP64 grid stages of one sample overlap the realization kernels of another, and the
+host work of a sample (its scatter-plan geometry, which the native builder computes with the GIL
+released) overlaps the device work of the others.  Samples are handed out longest first (their
+cost is bins x frequencies x realizations), so the pool drains evenly.
+
+The schedule (number of workers, and the waves of resident blocks the realization kernel's chunk
+count aims for) is picked by :func:`autotune`, which times a probe subset of the library at each
+candidate and caches the winner per device and workload class in ``_build/tuning.json``.
+
+Every sample's Philox key is derived from the library seed and the sample index alone, and every
+draw is keyed by (bin, realization, frequency), so the number of workers and the order in which they
+take samples change nothing: a batched run equals one :func:`lib_tools.run_model` call per sample with
+the same key, bit for bit.  The waves knob changes how the background sum is grouped into per-chunk
+partials, so it moves hc_bg in the last bits only (the draws and the loudest sources are unchanged).
+"""
+
+import json
+import os
+import queue
+import threading
+import time
+
+import numpy as np
+
+from .. import _device as D
+from .. import _native as N
+from . import DEF_NUM_FBINS, DEF_NUM_LOUDEST, DEF_PTA_DUR
+from .lib_tools import run_model
+
+_TUNING_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "_build", "tuning.json")
+_TUNING_LOCK = threading.Lock()
+
+#: (workers, waves) schedules the autotuner tries
+CANDIDATES = ((1, 2), (2, 2), (4, 2), (6, 2), (8, 2), (4, 1), (6, 1), (4, 3), (6, 3))
+
+
+def sample_seed(seed, index):
+    """Philox key of library sample ``index`` (independent of the schedule)."""
+    return int(np.random.SeedSequence([int(seed), int(index)]).generate_state(1, np.uint64)[0])
+
+
+def random_shapes(nsamples, lo=40, hi=91, reals_lo=100, reals_hi=1000, seed=0):
+    """Per-sample grid shapes (uniform integers in [lo, hi] per axis) and realization counts
+    (uniform integers in [reals_lo, reals_hi]) from ``np.random.default_rng(seed)``."""
+    rng = np.random.default_rng(seed)
+    shapes = rng.integers(lo, hi + 1, size=(nsamples, 3))
+    nreals = rng.integers(reals_lo, reals_hi + 1, size=nsamples)
+    return [tuple(int(v) for v in s) for s in shapes], [int(r) for r in nreals]
+
+
+class Job:
+    """One library sample: its index, parameters, grid shape, realization count and Philox key."""
+
+    __slots__ = ("index", "params", "shape", "nreals", "seed")
+
+    def __init__(self, index, params, shape, nreals, seed):
+        self.index, self.params, self.shape, self.nreals, self.seed = index, params, shape, nreals, seed
+
+    def cost(self, nfreqs):
+        m, q, z = self.shape
+        return (m - 1) * (q - 1) * (z - 1) * nfreqs * self.nreals
+
+
+def make_jobs(space, shapes=None, nreals=None, seed=0, indices=None):
+    """Jobs for the samples of ``space`` (all, or ``indices``).  ``shapes`` / ``nreals`` are per-sample
+    lists, or one value for every sample (default: the space's ``sam_shape`` and 100 realizations)."""
+    n = space.nsamples
+    indices = range(n) if indices is None else indices
+    jobs = []
+    for ii in indices:
+        shp = space.sam_shape if shapes is None else (shapes[ii] if np.ndim(shapes) == 2 else shapes)
+        if shp is None or np.isscalar(shp):
+            shp = (91, 81, 101) if shp is None else (int(shp),) * 3
+        nr = 100 if nreals is None else (nreals[ii] if np.ndim(nreals) == 1 else nreals)
+        jobs.append(Job(ii, space.param_dict(ii), tuple(int(v) for v in shp), int(nr), sample_seed(seed, ii)))
+    return jobs
+
+
+def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags):
+    """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: dict or None}
+    and {index: exception} for samples that failed."""
+    t = D.torch()
+    dev = D.device()
+    order = sorted(jobs, key=lambda j: -j.cost(nfreqs))
+    q = queue.Queue()
+    for job in order:
+        q.put(job)
+    results, errors = {}, {}
+    streams = [t.cuda.Stream(device=dev) for _ in range(workers)]
+
+    def work(stream):
+        with t.cuda.stream(stream):
+            while True:
+                try:
+                    job = q.get_nowait()
+                except queue.Empty:
+                    return
+                try:
+                    sam, hard = space.model_for_params(job.params, job.shape)
+                    results[job.index] = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
+                                                   nloudest=nloudest, seed=job.seed, **flags)
+                except Exception as err:   # a failed sample gives NaN rows, as in the reference's libraries
+                    results[job.index] = None
+                    errors[job.index] = err
+
+    threads = [threading.Thread(target=work, args=(s,), daemon=True) for s in streams]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for s in streams:
+        s.synchronize()
+    if errors and len(errors) == len(jobs):
+        raise next(iter(errors.values()))
+    return results, errors
+
+
+def _workload_class(jobs, nfreqs):
+    """A coarse key for the tuning cache: log2 of the mean per-sample cost and of the sample count."""
+    mean_cost = float(np.mean([j.cost(nfreqs) for j in jobs]))
+    return f"c{int(np.log2(max(mean_cost, 1.0)))}_n{int(np.log2(max(len(jobs), 1)))}"
+
+
+def _tuning_key(jobs, nfreqs):
+    t = D.torch()
+    return f"{t.cuda.get_device_name(D.device())}|{_workload_class(jobs, nfreqs)}"
+
+
+def _load_tuning():
+    try:
+        with open(_TUNING_PATH) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store_tuning(key, entry):
+    with _TUNING_LOCK:
+        table = _load_tuning()
+        table[key] = entry
+        try:
+            os.makedirs(os.path.dirname(_TUNING_PATH), exist_ok=True)
+            with open(_TUNING_PATH, "w") as fh:
+                json.dump(table, fh, indent=1, sort_keys=True)
+        except OSError:
+            pass
+
+
+def autotune(space, jobs, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST, pta_dur=DEF_PTA_DUR, flags=None,
+             candidates=CANDIDATES, probe=8, use_cache=True):
+    """Pick (workers, waves) for ``jobs`` by timing ``probe`` of them, spread over the cost range, at
+    each candidate schedule (after one untimed pass).  The scatter-plan cache is cleared before every
+    timed pass, so each candidate pays the per-sample host work a real library run pays.  Returns
+    ``dict(workers=, waves=, table={"w,v": draws/s})``; the winner is cached per device and workload
+    class."""
+    from ..sams import scatter
+    flags = dict(singles_flag=True) if flags is None else flags
+    key = _tuning_key(jobs, nfreqs)
+    if use_cache:
+        hit = _load_tuning().get(key)
+        if hit is not None:
+            return hit
+    ranked = sorted(jobs, key=lambda j: -j.cost(nfreqs))
+    pick = np.unique(np.linspace(0, len(ranked) - 1, min(probe, len(ranked))).round().astype(int))
+    probe_jobs = [ranked[i] for i in pick]
+    draws = float(sum(j.cost(nfreqs) for j in probe_jobs))
+    lib = N.load()
+    old_waves = lib.hgb_get_bulk_waves()
+    _run_jobs(space, probe_jobs, 1, nfreqs, nloudest, pta_dur, flags)   # untimed: lazy setup, allocator warm-up
+    table = {}
+    try:
+        for workers, waves in candidates:
+            N.check(lib.hgb_set_bulk_waves(int(waves)), "hgb_set_bulk_waves")
+            scatter.clear_plan_cache()
+            D.torch().cuda.synchronize()
+            t0 = time.perf_counter()
+            _run_jobs(space, probe_jobs, workers, nfreqs, nloudest, pta_dur, flags)
+            D.torch().cuda.synchronize()
+            table[f"{workers},{waves}"] = draws / (time.perf_counter() - t0)
+    finally:
+        N.check(lib.hgb_set_bulk_waves(old_waves), "hgb_set_bulk_waves")
+    best = max(table, key=table.get)
+    workers, waves = (int(v) for v in best.split(","))
+    entry = dict(workers=workers, waves=waves, table=table, probe=len(probe_jobs))
+    _store_tuning(key, entry)
+    return entry
+
+
+def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST,
+                pta_dur=DEF_PTA_DUR, seed=0, singles_flag=True, gwb_flag=False, params_flag=False,
+                details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None):
+    """Evaluate the samples of ``space`` (all, or ``indices``) on this GPU; returns the list of
+    per-sample :func:`lib_tools.run_model` dicts in sample order (``None`` for a failed sample), the
+    input that :func:`lib_tools.write_library` takes.
+
+    ``shapes`` / ``nreals``: per-sample lists or one value each (see :func:`make_jobs`).  ``seed``
+    keys every sample's realizations (:func:`sample_seed`).  ``workers`` / ``waves`` fix the
+    schedule; otherwise it comes from :func:`autotune` (``tune=True``) or defaults to (3, 2).
+    ``stats``, when a dict, receives the schedule, wall time, sample count, realizations and draws.
+    """
+    flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag)
+    jobs = make_jobs(space, shapes, nreals, seed, indices)
+    if not jobs:
+        return []
+    tuned = None
+    if workers is None or waves is None:
+        if tune:
+            tuned = autotune(space, jobs, nfreqs, nloudest, pta_dur, flags)
+            workers = tuned["workers"] if workers is None else workers
+            waves = tuned["waves"] if waves is None else waves
+        else:
+            workers = 3 if workers is None else workers
+            waves = 2 if waves is None else waves
+    lib = N.load()
+    old_waves = lib.hgb_get_bulk_waves()
+    N.check(lib.hgb_set_bulk_waves(int(waves)), "hgb_set_bulk_waves")
+    try:
+        D.torch().cuda.synchronize()
+        t0 = time.perf_counter()
+        results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags)
+        D.torch().cuda.synchronize()
+        wall = time.perf_counter() - t0
+    finally:
+        N.check(lib.hgb_set_bulk_waves(old_waves), "hgb_set_bulk_waves")
+    if stats is not None:
+        stats.update(workers=int(workers), waves=int(waves), seconds=wall, samples=len(jobs),
+                     failed=len(errors), realizations=int(sum(j.nreals for j in jobs)),
+                     draws=float(sum(j.cost(nfreqs) for j in jobs)), tuning=tuned,
+                     errors={k: repr(v) for k, v in errors.items()})
+    return [results.get(j.index) for j in sorted(jobs, key=lambda j: j.index)]

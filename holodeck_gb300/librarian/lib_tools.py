@@ -1,14 +1,181 @@
-"""GPU versions of holodeck/librarian/lib_tools.py:714-943 (``run_model``, ``_calc_model_details``)
-and a writer of the combined library (librarian/combine.py:86-260) as ``.npz``, or HDF5 when h5py
-is importable."""
+"""GPU versions of holodeck/librarian/lib_tools.py:714-943 (``run_model``, ``_calc_model_details``),
+the parameter-space classes that feed library runs (lib_tools.py:34-711: ``_Param_Space``,
+``PD_Uniform``, ``PD_Normal``), and a writer of the combined library (librarian/combine.py:86-260) as
+``.npz``, or HDF5 when h5py is importable."""
+
+import abc
+import logging
 
 import numpy as np
+import scipy as sp
+import scipy.stats  # noqa: F401  (sp.stats.qmc, sp.stats.norm)
 
 from .. import _device as D
 from .. import _native as N
 from .. import gravwaves, hardening, single_sources, utils
 from ..constants import YR
 from . import DEF_NUM_FBINS, DEF_NUM_LOUDEST, DEF_NUM_REALS, DEF_PTA_DUR
+
+
+class _Param_Space(abc.ABC):
+    """A library's parameter space (lib_tools.py:34-464): named parameter distributions, a Latin
+    hypercube of ``nsamples`` draws over them, and the model (SAM + hardening) of any sample.
+
+    The draws are scipy's ``LatinHypercube(d=P, strength=1, seed=seed)`` mapped through each
+    distribution, exactly as lib_tools.py:136-141 makes them.  Subclasses set ``DEFAULTS`` and
+    implement ``_init_sam(sam_shape, params)`` and ``_init_hard(sam, params)``.
+    """
+
+    DEFAULTS = {}
+
+    def __init__(self, parameters, log=None, nsamples=None, sam_shape=None, seed=None, random_state=None):
+        log = logging.getLogger("holodeck_gb300") if log is None else log
+        try:
+            nparameters = len(parameters)
+            assert nparameters > 0
+        except (TypeError, AssertionError) as err:
+            log.exception("`parameters` must be a list of `_Param_Dist` subclasses!")
+            raise err
+        for param in parameters:
+            if not isinstance(param, _Param_Dist):
+                err = f"{param.name}: {param} is not a `_Param_Dist` object!"
+                log.exception(err)
+                raise ValueError(err)
+        if nsamples is None:
+            uniform_samples = None
+            param_samples = None
+        else:
+            lhc = sp.stats.qmc.LatinHypercube(d=nparameters, strength=1, seed=seed)
+            uniform_samples = lhc.random(n=nsamples)     # (S, P)
+            param_samples = np.zeros_like(uniform_samples)
+            for ii, param in enumerate(parameters):
+                param_samples[:, ii] = param(uniform_samples[:, ii])
+        self._log = log
+        self._nparameters = nparameters
+        self._nsamples = nsamples
+        self._seed = seed
+        self._random_state = random_state
+        self.sam_shape = sam_shape
+        self.param_names = [param.name for param in parameters]
+        self.param_samples = param_samples
+        self._parameters = parameters
+        self._uniform_samples = uniform_samples
+
+    def model_for_params(self, params, sam_shape=None):
+        """(sam, hard) for a dict of parameter values; unnamed settings take ``DEFAULTS`` (lib_tools.py:156-213)."""
+        if sam_shape is None:
+            sam_shape = self.sam_shape
+        settings = self.DEFAULTS.copy()
+        for name, value in params.items():
+            settings[name] = value
+        sam = self._init_sam(sam_shape, settings)
+        hard = self._init_hard(sam, settings)
+        return sam, hard
+
+    def param_dict(self, samp_num):
+        return {nn: pp for nn, pp in zip(self.param_names, self.param_samples[samp_num])}
+
+    @property
+    def extrema(self):
+        return np.asarray([dd.extrema for dd in self._parameters])
+
+    @property
+    def name(self):
+        return self.__class__.__name__
+
+    @property
+    def lib_shape(self):
+        return self.param_samples.shape
+
+    @property
+    def nsamples(self):
+        return self._nsamples
+
+    @property
+    def nparameters(self):
+        return self._nparameters
+
+    def model_for_sample_number(self, samp_num, sam_shape=None):
+        return self.model_for_params(self.param_dict(samp_num), sam_shape)
+
+    def normalized_params(self, vals):
+        """Parameters for fractional coordinates in [0, 1] (``None`` takes the default), lib_tools.py:409-451."""
+        if np.ndim(vals) == 0:
+            vals = self.nparameters * [vals]
+        assert len(vals) == self.nparameters
+        assert np.all([(vv is None) or np.isfinite(vv) for vv in vals]), f"Not all `vals` are finite!  {vals}"
+        return {pname: (param.default if vv is None else param(vv))
+                for pname, param, vv in zip(self.param_names, self._parameters, vals)}
+
+    def default_params(self):
+        return {param.name: param.default for param in self._parameters}
+
+    @abc.abstractmethod
+    def _init_sam(self, sam_shape, params):
+        pass
+
+    @abc.abstractmethod
+    def _init_hard(self, sam, params):
+        pass
+
+
+class _Param_Dist(abc.ABC):
+    """A parameter distribution: maps uniform [0, 1] draws to parameter values (lib_tools.py:467-517)."""
+
+    def __init__(self, name, default=None, clip=None):
+        if clip is not None:
+            assert len(clip) == 2
+        self._clip = clip
+        self._name = name
+        self._default = default
+
+    def __call__(self, xx):
+        rv = self._dist_func(xx)
+        if self._clip is not None:
+            rv = np.clip(rv, *self._clip)
+        return rv
+
+    @abc.abstractmethod
+    def _dist_func(self, xx):
+        pass
+
+    @property
+    def extrema(self):
+        return self(np.asarray([0.0, 1.0]))
+
+    @property
+    def name(self):
+        return self._name
+
+    @property
+    def default(self):
+        return self._default if self._default is not None else self(0.5)
+
+
+class PD_Uniform(_Param_Dist):
+    """Uniform on [lo, hi] (lib_tools.py:520-530)."""
+
+    def __init__(self, name, lo, hi, **kwargs):
+        super().__init__(name, **kwargs)
+        self._lo = lo
+        self._hi = hi
+
+    def _dist_func(self, xx):
+        return self._lo + (self._hi - self._lo) * xx
+
+
+class PD_Normal(_Param_Dist):
+    """Normal(mean, stdev) through its inverse CDF (lib_tools.py:547-578)."""
+
+    def __init__(self, name, mean, stdev, clip=None, **kwargs):
+        assert stdev > 0.0
+        super().__init__(name, clip=clip, **kwargs)
+        self._mean = mean
+        self._stdev = stdev
+        self._dist = sp.stats.norm(loc=mean, scale=stdev)
+
+    def _dist_func(self, xx):
+        return self._dist.ppf(xx)
 
 
 def _calc_model_details_device(edges, redz_final, number, h2fdf=None, cosmo=None):
@@ -76,7 +243,7 @@ def run_model(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_N
         if log is not None:
             log.exception(err)
         raise RuntimeError(err)
-    redz_final, diff_num = sam._dbn_device(hard, fobs_orb_cents)
+    redz_final, diff_num = sam._dbn_scheduled(hard, fobs_orb_cents)
     edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
     number, h2fdf = sam._number_and_strain(fobs_orb_edges, diff_num, redz_final)
     if details_flag:

@@ -26,18 +26,6 @@ GPF_USES_MTOT = False        #: sam.py:58
 GMT_USES_MTOT = False        #: sam.py:59
 
 
-_AUX_STREAMS = {}
-
-
-def _aux_stream(device):
-    """One second stream per device for grid stages that can overlap the current stream's work."""
-    t = D.torch()
-    key = t.device(device).index
-    if key not in _AUX_STREAMS:
-        _AUX_STREAMS[key] = t.cuda.Stream(device=device)
-    return _AUX_STREAMS[key]
-
-
 class Semi_Analytic_Model:
     """Semi-analytic model of MBH-binary populations on an (mtot, mrat, redz) grid (sam.py:66-234)."""
 
@@ -212,7 +200,7 @@ class Semi_Analytic_Model:
         dens, gmt_time, redz_prime = self._static_density_launch()
         mt, mr, rz = self._edges_device()
         main = t.cuda.current_stream()
-        side = _aux_stream(main.device)
+        side = D.side_stream("dbn_walk", main.device)
         static_done = t.cuda.Event()
         static_done.record(main)
         side.wait_event(static_done)
@@ -228,6 +216,13 @@ class Semi_Analytic_Model:
         diff_num.record_stream(main)
         return sam_cyutils.dbn_2pwl_device(fobs_orb, hard, dens, mt, mr, rz, gmt_time, cosmo=self._cosmo, phase=2,
                                            out=(redz_final, diff_num))
+
+    def _dbn_scheduled(self, hard, fobs_orb):
+        """_dbn_device, overlapping the separation-step walk with the scatter where that applies."""
+        if (self._density_t is None and self._gmt is not None and isinstance(hard, hardening.Fixed_Time_2PL_SAM)
+                and self._mmbulge._scatter_dex > 0.0):
+            return self._dbn_2pwl_overlapped(hard, fobs_orb)
+        return self._dbn_device(hard, fobs_orb)
 
     def dynamic_binary_number_at_fobs(self, hard, fobs_orb, use_cython=True, **kwargs):
         """(grid, dnum, redz_final) like sam.py:400-466 (``use_cython`` is accepted and ignored)."""
@@ -250,11 +245,7 @@ class Semi_Analytic_Model:
         fobs_gw_cents = utils.midpoints(fobs_gw_edges)
         fobs_orb_edges = fobs_gw_edges / 2.0
         fobs_orb_cents = fobs_gw_cents / 2.0
-        if (self._density_t is None and self._gmt is not None and isinstance(hard, hardening.Fixed_Time_2PL_SAM)
-                and self._mmbulge._scatter_dex > 0.0):
-            redz_final, diff_num = self._dbn_2pwl_overlapped(hard, fobs_orb_cents)
-        else:
-            redz_final, diff_num = self._dbn_device(hard, fobs_orb_cents)
+        redz_final, diff_num = self._dbn_scheduled(hard, fobs_orb_cents)
         number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final)
         if params:
             edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]

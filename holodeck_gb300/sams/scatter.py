@@ -5,8 +5,10 @@ The grid geometry (triangulation, interpolation stencils, redistribution matrix)
 the device; every call then runs the per-slice kernels of ``csrc/hgb_scatter.cu``.
 """
 
+import collections
 import ctypes
 import logging
+import threading
 import warnings
 
 import numpy as np
@@ -25,7 +27,9 @@ _DTYPES = dict(pts=np.float64, tri=np.int32, tri_kappa=np.float64, vtx_qinv=np.f
                back_idx=np.int32, back_t=np.float64, back_w=np.float64, lv_nbr_ptr=np.int32, lv_nbr=np.int32,
                lv_nbr_w=np.float64, lv_qinv=np.float64)
 
-_PLANS = {}
+_PLANS = collections.OrderedDict()   # least recently used first
+_PLAN_CACHE_MAX = 8                   # plans kept per process (a 91 x 81 plan holds about 60 MB)
+_PLAN_LOCK = threading.Lock()
 
 
 def host_plan(mtot, mrat, scatter, refine=4):
@@ -84,11 +88,26 @@ class DevicePlan:
 def device_plan(mtot, mrat, scatter, refine=4):
     key = (np.asarray(mtot, dtype=np.float64).tobytes(), np.asarray(mrat, dtype=np.float64).tobytes(),
            float(scatter), int(refine), str(D.device()))
-    plan = _PLANS.get(key)
-    if plan is None:
-        plan = DevicePlan(mtot, mrat, scatter, refine)
-        _PLANS[key] = plan
+    with _PLAN_LOCK:
+        plan = _PLANS.get(key)
+        if plan is not None:
+            _PLANS.move_to_end(key)
+            return plan
+    # built outside the lock (the native builder releases the GIL), so workers build plans concurrently;
+    # a caller keeps its plan alive until its kernels have run, whatever the cache evicts
+    plan = DevicePlan(mtot, mrat, scatter, refine)
+    with _PLAN_LOCK:
+        plan = _PLANS.setdefault(key, plan)
+        _PLANS.move_to_end(key)
+        while len(_PLANS) > _PLAN_CACHE_MAX:
+            _PLANS.popitem(last=False)
     return plan
+
+
+def clear_plan_cache():
+    """Drop the cached plans (their device memory is freed once no call holds them)."""
+    with _PLAN_LOCK:
+        _PLANS.clear()
 
 
 def add_scatter_to_masses_device(mtot, mrat, dens, scatter, refine=4):

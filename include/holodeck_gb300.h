@@ -337,6 +337,14 @@ int hgb_model_details(const double *number, const double *h2fdf, const double *r
 int hgb_bulk_timing(int enable);
 float hgb_bulk_last_ms(void);
 
+/* No reference counterpart.  Schedule knob of the realization kernels, set by the batched-library
+ * autotuner: the chunk count of k_bulk aims for `waves` waves of resident blocks (six per SM) over the
+ * device's SMs (default 2).  Applies to every later launch in the process; workspace sizes are
+ * always computed for HGB_BULK_WAVES_MAX, so changing it never invalidates a workspace. */
+#define HGB_BULK_WAVES_MAX 4
+int hgb_set_bulk_waves(int waves);   /* 1 <= waves <= HGB_BULK_WAVES_MAX, else HGB_ERR_INVALID_ARGUMENT */
+int hgb_get_bulk_waves(void);
+
 /* Second-pass GWB without the loudest split.  Replaces cyutils.sam_poisson_gwb,
  * cyutils.pyx:854-897; gwb is (F, R).  replay[(b*F + f)*R + r] in REPLAY mode (no workspace needed). */
 size_t hgb_sam_poisson_gwb_workspace_bytes(long n_bins, int n_freq, int nreals);

@@ -206,6 +206,27 @@ def case_params():
     save("ref_params.npz", **out, ncases=2, hard_time=3.0 * GYR)
 
 
+def case_param_space():
+    """Latin-hypercube library samples of ``PS_Classic_Phenom_Uniform`` (lib_tools.py:49-154,
+    param_spaces_classic.py:12-107) and the grids of two of its models at a small shape, which pin the
+    mapping from library parameters to SAM and hardening settings."""
+    from holodeck.librarian import param_spaces_classic as psc
+    space = psc.PS_Classic_Phenom_Uniform(nsamples=8, sam_shape=(10, 11, 12), seed=0)
+    out = dict(param_samples=space.param_samples, uniform_samples=space._uniform_samples,
+               param_names=np.array(space.param_names), extrema=space.extrema)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.03 * YR, 4)
+    fobs_orb_edges = fobs_gw_edges / 2.0
+    for ii in (0, 5):
+        sam, hard = space.model_for_sample_number(ii)
+        redz_final, dnum = sam_cyutils.dynamic_binary_number_at_fobs(fobs_gw_cents / 2.0, sam, hard, holo.cosmo)
+        number = sam_cyutils.integrate_differential_number_3dx1d([sam.mtot, sam.mrat, sam.redz, fobs_orb_edges], dnum)
+        out.update({f"s{ii}_mtot": sam.mtot, f"s{ii}_mrat": sam.mrat, f"s{ii}_redz": sam.redz,
+                    f"s{ii}_density": sam.static_binary_density, f"s{ii}_norm": hard._norm,
+                    f"s{ii}_redz_final": redz_final, f"s{ii}_number": number})
+    out["fobs_gw_edges"] = fobs_gw_edges
+    save("ref_param_space.npz", **out)
+
+
 def case_details():
     """``_calc_model_details`` (librarian/lib_tools.py:845-943) and ``run_model``'s deterministic keys."""
     from holodeck.librarian import lib_tools
@@ -256,6 +277,7 @@ def main(only=None):
     case_cfg1()
     case_params()
     case_details()
+    case_param_space()
 
 
 if __name__ == "__main__":

@@ -1,0 +1,118 @@
+"""Library parameter spaces and batched library runs.
+
+The Latin-hypercube samples and the parameter -> model mapping of PS_Classic_Phenom_Uniform
+(librarian/lib_tools.py:34-541, librarian/param_spaces_classic.py:12-107) against the reference's own
+output (``ref_param_space.npz``); the batched runner against one run_model call per sample.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+
+def _significant_rel(a, b, floor=1e-12):
+    a, b = np.asarray(a), np.asarray(b)
+    m = np.abs(b) > floor * np.abs(b).max()
+    return float((np.abs(a[m] - b[m]) / np.abs(b[m])).max())
+
+
+def test_param_space_samples_match_reference():
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform
+    g = load_golden("ref_param_space.npz")
+    space = PS_Classic_Phenom_Uniform(nsamples=8, sam_shape=(10, 11, 12), seed=0)
+    assert list(space.param_names) == [str(x) for x in g["param_names"]]
+    assert np.array_equal(space._uniform_samples, g["uniform_samples"])
+    assert np.array_equal(space.param_samples, g["param_samples"])
+    assert np.array_equal(space.extrema, g["extrema"])
+    assert space.lib_shape == (8, 6) and space.nparameters == 6
+    p = space.normalized_params([0.5, None, 0.0, 1.0, 0.25, 0.5])
+    assert p["gsmf_phi0_log10"] == -2.5 and p["mmb_mamp_log10"] == 7.6 and p["mmb_scatter_dex"] == 0.9
+    assert p["gsmf_mchar0_log10"] == 11.5   # default = the distribution at 0.5
+
+
+def test_jobs_seeds_and_shapes():
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
+    shapes, nreals = batch.random_shapes(512, seed=0)
+    arr = np.array(shapes)
+    assert arr.min() >= 40 and arr.max() <= 91 and min(nreals) >= 100 and max(nreals) <= 1000
+    assert batch.random_shapes(512, seed=0) == (shapes, nreals)
+    space = PS_Classic_Phenom_Uniform(nsamples=5, seed=1)
+    jobs = batch.make_jobs(space, shapes[:5], nreals[:5], seed=3)
+    again = batch.make_jobs(space, shapes[:5], nreals[:5], seed=3, indices=[4, 2, 0, 1, 3])
+    by_index = {j.index: j.seed for j in again}
+    assert [j.seed for j in jobs] == [by_index[i] for i in range(5)]
+    assert len({j.seed for j in jobs}) == 5
+    m, q, z = shapes[0]
+    assert jobs[0].cost(40) == (m - 1) * (q - 1) * (z - 1) * 40 * nreals[0]
+    one = batch.make_jobs(space, (12, 13, 14), 7)
+    assert all(j.shape == (12, 13, 14) and j.nreals == 7 for j in one)
+
+
+@pytest.mark.gpu
+def test_param_space_models_match_reference(built_lib):
+    """Two library samples (with M-Mbulge scatter) built from their parameters: density, hardening
+    normalisation, final redshifts and bin numbers against the reference's own models."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform
+    from holodeck_gb300.sams import sam_cyutils
+    g = load_golden("ref_param_space.npz")
+    space = PS_Classic_Phenom_Uniform(nsamples=8, sam_shape=(10, 11, 12), seed=0)
+    fe = g["fobs_gw_edges"]
+    fc = 0.5 * (fe[1:] + fe[:-1])
+    for ii in (0, 5):
+        k = f"s{ii}_"
+        settings = {**space.DEFAULTS, **space.param_dict(ii)}
+        sam = space._init_sam(space.sam_shape, settings)
+        assert sam._mmbulge._scatter_dex > 0.0
+        # np.logspace may differ in the last bit between hosts: use the reference's own edges
+        sam.mtot, sam.mrat, sam.redz = g[k + "mtot"], g[k + "mrat"], g[k + "redz"]
+        hard = space._init_hard(sam, settings)
+        assert rel_err(hard._norm, g[k + "norm"]) < 1e-9, ii
+        dens = sam.static_binary_density
+        assert np.array_equal(dens == 0.0, g[k + "density"] == 0.0), ii
+        assert _significant_rel(dens, g[k + "density"]) < 1e-9, ii
+        rf, dn = sam_cyutils.dynamic_binary_number_at_fobs(fc / 2.0, sam, hard)
+        assert np.array_equal(rf == -1.0, g[k + "redz_final"] == -1.0), ii
+        assert rel_err(rf, g[k + "redz_final"]) < 1e-9, ii
+        number = sam_cyutils.integrate_differential_number_3dx1d(
+            [sam.mtot, sam.mrat, sam.redz, fe / 2.0], dn)
+        assert _significant_rel(number, g[k + "number"]) < 1e-9, ii
+
+
+@pytest.mark.gpu
+def test_batched_library_equals_per_sample_runs(built_lib):
+    """run_library on several workers gives each sample's run_model result bit for bit; the waves knob
+    moves hc_bg in the last bits only."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch, lib_tools
+    space = PS_Classic_Phenom_Uniform(nsamples=6, seed=2)
+    shapes, nreals = batch.random_shapes(6, lo=10, hi=16, reals_lo=5, reals_hi=20, seed=4)
+    stats = {}
+    out = batch.run_library(space, shapes, nreals, nfreqs=5, nloudest=3, seed=11, workers=3, waves=2,
+                            gwb_flag=True, stats=stats)
+    assert stats["samples"] == 6 and stats["failed"] == 0 and stats["workers"] == 3
+    assert stats["realizations"] == sum(nreals)
+    for ii in range(6):
+        sam, hard = space.model_for_sample_number(ii, sam_shape=shapes[ii])
+        ref = lib_tools.run_model(sam, hard, nfreqs=5, nreals=nreals[ii], nloudest=3, gwb_flag=True,
+                                  seed=batch.sample_seed(11, ii))
+        for key in ("hc_ss", "hc_bg", "gwb", "fobs_edges"):
+            assert np.array_equal(out[ii][key], ref[key]), (ii, key)
+    one = batch.run_library(space, shapes, nreals, nfreqs=5, nloudest=3, seed=11, workers=1, waves=1)
+    for ii in range(6):
+        assert np.array_equal(one[ii]["hc_ss"], out[ii]["hc_ss"])
+        assert rel_err(one[ii]["hc_bg"], out[ii]["hc_bg"]) < 1e-13
+
+
+@pytest.mark.gpu
+def test_autotune_times_every_candidate(built_lib):
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
+    from holodeck_gb300 import _native as N
+    space = PS_Classic_Phenom_Uniform(nsamples=4, seed=5)
+    shapes, nreals = batch.random_shapes(4, lo=12, hi=18, reals_lo=10, reals_hi=30, seed=6)
+    jobs = batch.make_jobs(space, shapes, nreals)
+    before = N.load().hgb_get_bulk_waves()
+    res = batch.autotune(space, jobs, nfreqs=4, nloudest=2, candidates=((1, 2), (2, 1)), probe=3, use_cache=False)
+    assert set(res["table"]) == {"1,2", "2,1"} and all(v > 0 for v in res["table"].values())
+    assert (res["workers"], res["waves"]) in ((1, 2), (2, 1))
+    assert N.load().hgb_get_bulk_waves() == before
+    assert batch.autotune(space, jobs, nfreqs=4, nloudest=2, candidates=((1, 2),), probe=3)["workers"] in (1, 2)
