@@ -10,11 +10,14 @@ Poisson realizations with the loudest split).  value = realizations / s.
 
 The line also carries ``batched``: a whole library of 512 Latin-hypercube samples of
 PS_Classic_Phenom_Uniform, each on its own grid (40-91 per axis) with its own realization count
-(100-1000), run through the batched library API (realizations/s over the library).
+(100-1000), run through the batched library API (realizations/s over the library), and
+``emulator``: the MLP ensemble trained on a GPU-SAM library of the same space at the default grid,
+its held-out accuracy and query time against the plain GPU SAM's time for the same query.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
     python bench.py --stages        # per-stage device times
     python bench.py --batched       # only the batched-library measurement
+    python bench.py --emulator [--emulator-samples 20000]   # only the emulator measurement
     python bench.py --profile --nfreqs K   # one untimed evaluation (the program ncu captures)
 
 --impl reference times the CPU restatement of the reference path (the oracle) on the host cores.
@@ -234,6 +237,7 @@ def run_gpu(args):
         pass
 
     batched = run_batched(args, rank, world) if args.batched_samples > 0 else None
+    emulator = run_emulator(args) if (args.emulator_samples > 0 and rank == 0) else None
     cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
     if rank == 0:
         line = {
@@ -258,6 +262,7 @@ def run_gpu(args):
             "clocks": clk,
             "cpu_baseline": cpu,
             "batched": batched,
+            "emulator": emulator,
         }
         print(json.dumps(line))
     if world > 1:
@@ -302,6 +307,79 @@ def run_batched(args, rank=0, world=1):
             "speedup_vs_one_worker_in_probe": (best / one) if (best and one) else None,
             "e2e": "host parameters in, host hc_ss / hc_bg out; per-sample scatter plans built on the host "
                    "inside the timed region", "d2h_bytes": int(d2h)}
+
+
+EMU_CONFIG = ("learned emulator: 4-member ensemble of MLPs 6 -> 4x256 (SiLU) -> 40 x (5/50/95th percentile "
+              "log10 hc, median log10 loudest-source hc), bf16 weights and activations, fp32 accumulation on "
+              "tcgen05, AdamW; trained on Latin-hypercube samples (seed 0) of PS_Classic_Phenom_Uniform at the "
+              "91x81x101 grid with 500 realizations, tested on held-out samples (seed 1)")
+
+
+def run_emulator(args):
+    """Train the emulator on a GPU-SAM library and measure it against the plain GPU SAM: held-out
+    accuracy (and the nearest-library-sample answer a user has without the network, and the
+    realization-noise floor of the held-out truth), query latency through the CUDA-graph path, and
+    the plain GPU SAM's time for the same query."""
+    import torch
+    from holodeck_gb300 import emulator as EM
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform
+    n_tr = args.emulator_samples
+    n_te = max(64, n_tr // 10)
+    sp_tr = PS_Classic_Phenom_Uniform(nsamples=n_tr, seed=0)
+    sp_te = PS_Classic_Phenom_Uniform(nsamples=n_te, seed=1)
+    lib_stats = {}
+    cache = args.emulator_cache
+    if cache and os.path.exists(cache):
+        with np.load(cache) as z:
+            assert np.array_equal(z["params_train"], sp_tr.param_samples), "cache holds another library"
+            y_tr, y_te, y_te2 = z["y_train"], z["y_test"], z["y_test2"]
+            lib_stats["seconds"] = float(z["library_seconds"])
+    else:
+        y_tr = EM.training_library(sp_tr, seed=2, stats=lib_stats)
+        y_te = EM.training_library(sp_te, seed=3)
+        y_te2 = EM.training_library(sp_te, seed=4)         # same held-out models, other realizations
+        if cache:
+            np.savez(cache, params_train=sp_tr.param_samples, params_test=sp_te.param_samples, y_train=y_tr,
+                     y_test=y_te, y_test2=y_te2, library_seconds=lib_stats["seconds"])
+    ok = np.all(np.isfinite(y_tr), axis=(1, 2))
+    emu = EM.Emulator(sp_tr, nfreqs=NFREQ, members=4, width=256, depth=4, seed=0)
+    steps_per_epoch = max(1, int(ok.sum()) // 512)
+    epochs = max(50, -(-args.emulator_steps // steps_per_epoch))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hist = emu.fit(sp_tr.param_samples[ok], y_tr[ok], epochs=epochs, batch=512, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    mean, spread, inside = emu.predict(sp_te.param_samples)
+    good = np.all(np.isfinite(y_te), axis=(1, 2)) & np.all(np.isfinite(y_te2), axis=(1, 2))
+    err = np.abs(mean - y_te)[good]
+    u_tr, u_te = emu.unit(sp_tr.param_samples[ok]), emu.unit(sp_te.param_samples)
+    nn = np.argmin(((u_te[:, None, :] - u_tr[None, :, :]) ** 2).sum(-1), axis=1)
+    err_nn = np.abs(y_tr[ok][nn] - y_te)[good]
+    noise = np.abs(y_te - y_te2)[good] / np.sqrt(2.0)
+    g1, gb = emu.graphed(1), emu.graphed(1024)
+    q1 = sp_te.param_samples[:1]
+    qb = np.resize(sp_te.param_samples, (1024, sp_te.param_samples.shape[1]))
+    t_q1 = EM.timed(g1, q1, repeat=50)
+    t_qb = EM.timed(gb, qb, repeat=20)
+    solve = EM.sam_fallback(sp_tr, sam_shape=SHAPE, nreals=500, nfreqs=NFREQ, seed=5)
+    t_plain = EM.timed(solve, q1[0], repeat=3)
+    names = list(EM.STATS)
+
+    def med(a):
+        return {nm: float(np.median(a[..., k])) for k, nm in enumerate(names)}
+
+    return {"workload": EMU_CONFIG, "train_samples": int(ok.sum()), "test_samples": int(good.sum()),
+            "library_seconds": lib_stats.get("seconds"), "library_samples_per_s": n_tr / lib_stats["seconds"],
+            "train_seconds": t_train, "train_steps": epochs * steps_per_epoch, "final_loss": hist[-1],
+            "median_abs_dlog10": med(err), "p95_abs_dlog10": {nm: float(np.percentile(err[..., k], 95))
+                                                             for k, nm in enumerate(names)},
+            "nearest_sample_median_abs_dlog10": med(err_nn), "realization_noise_median_dlog10": med(noise),
+            "ensemble_spread_median_dex": float(np.median(spread)),
+            "flagged_fraction_at_0.05dex": float(np.mean(spread > 0.05)),
+            "query_s_batch1": t_q1, "query_s_per_sample_batch1024": t_qb / 1024,
+            "plain_gpu_sam_s": t_plain, "speedup_vs_plain_batch1": t_plain / t_q1,
+            "speedup_vs_plain_batch1024": t_plain / (t_qb / 1024)}
 
 
 # ------------------------------------------------------------------------------------------------
@@ -472,11 +550,21 @@ def main():
     ap.add_argument("--batched-samples", type=int, default=512,
                     help="library samples of the batched measurement carried by the bench line (0: skip)")
     ap.add_argument("--batched", action="store_true", help="only the batched-library measurement")
+    ap.add_argument("--emulator-samples", type=int, default=2048,
+                    help="training samples of the emulator measurement carried by the bench line (0: skip)")
+    ap.add_argument("--emulator-steps", type=int, default=6000, help="emulator training steps (batch 512)")
+    ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
+    ap.add_argument("--emulator-cache", default=None,
+                    help=".npz holding the emulator's training library statistics (written when absent)")
     args = ap.parse_args()
     if args.batched and args.impl != "reference":
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps({"metric": METRIC, "batched": run_batched(args)}))
+    elif args.emulator and args.impl != "reference":
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps({"metric": METRIC, "emulator": run_emulator(args)}))
     elif args.profile:
         run_profile(args)
     elif args.stages:

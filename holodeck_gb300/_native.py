@@ -80,6 +80,15 @@ class HgbScatterPlan(ctypes.Structure):
                 [("grad_tol", _d), ("grad_maxiter", _i)])
 
 
+MLP_MAX_LAYERS = 8       # HGB_MLP_MAX_LAYERS
+MLP_SPLIT_ROWS = 128     # HGB_MLP_SPLIT_ROWS
+
+
+class HgbMlp(ctypes.Structure):
+    _fields_ = [("n_layers", _i), ("n_members", _i), ("dims", _i * (MLP_MAX_LAYERS + 1)), ("params", _p),
+                ("weights", _p)]
+
+
 #: (name, restype, argtypes) for every exported entry point
 SIGNATURES = [
     ("hgb_version", _i, []),
@@ -120,6 +129,14 @@ SIGNATURES = [
     ("hgb_bulk_last_ms", ctypes.c_float, []),
     ("hgb_set_bulk_waves", _i, [_i]),
     ("hgb_get_bulk_waves", _i, []),
+    ("hgb_mlp_param_count", _l, [ctypes.POINTER(HgbMlp)]),
+    ("hgb_mlp_weight_count", _l, [ctypes.POINTER(HgbMlp)]),
+    ("hgb_mlp_forward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _p]),
+    ("hgb_mlp_backward_workspace_bytes", _sz, [ctypes.POINTER(HgbMlp), _i]),
+    ("hgb_mlp_backward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _l, _p, _p, _p, _sz, _p, _p]),
+    ("hgb_mlp_adamw", _i, [ctypes.POINTER(HgbMlp), _p, _p, _p, _p, _p, _i, ctypes.c_float, ctypes.c_float,
+                           ctypes.c_float, ctypes.c_float, ctypes.c_float, _p]),
+    ("hgb_mlp_pack_weights", _i, [ctypes.POINTER(HgbMlp), _p, _p, _p]),
     ("hgb_sam_poisson_gwb_workspace_bytes", _sz, [_l, _i, _i]),
     ("hgb_sam_poisson_gwb", _i, [_p, _p, _l, _i, _i, _i, _u64, _p, _p, _p, _sz, _p, _p]),
 ]
@@ -176,7 +193,7 @@ KERNELS_PER_CALL = {
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
-    "hgb_loudest_hc_and_par_from_sorted": 6,
+    "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1,
 }
 _launches = [0]
 _launch_lock = threading.Lock()
@@ -188,6 +205,12 @@ def reset_launch_count():
 
 def launch_count():
     return _launches[0]
+
+
+def add_launches(n):
+    """Count kernels of a call whose launch count depends on its arguments."""
+    with _launch_lock:
+        _launches[0] += int(n)
 
 
 def call(name, *args):

@@ -1,0 +1,643 @@
+// Emulator MLP: forward, backward and AdamW for an ensemble of small multilayer perceptrons that map
+// library parameters to per-frequency strain statistics.  No reference counterpart (the reference's
+// emulators are Gaussian processes, holodeck/gps/); the training data are libraries the GPU SAM
+// itself writes.
+//
+// Network: E members, each K_0 (inputs, padded to 16) -> N_0 -> ... -> N_{L-1} (outputs), SiLU after
+// every layer but the last.  Weights bf16, row-major [N_l][K_l]; biases and master weights fp32.
+// Activations between layers are bf16, pre-activations and outputs fp32, and every product is
+// accumulated in fp32.
+//
+// All three contractions (forward Y = X W^T, input gradient dX = dZ W, weight gradient
+// dW = dZ^T X) run on one tensor-core core: a CTA of 128 threads owns a 128-row output tile with up
+// to 256 columns in tensor memory (tcgen05.alloc, 256 columns of fp32), stages 64-wide slices of the
+// reduction axis of both operands in shared memory in the canonical no-swizzle K-major layout
+// (8 x 16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row groups 1024 B apart), and
+// one elected thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = 128, K = 16 per
+// instruction) and commits them to an mbarrier; the epilogue reads the accumulator back with
+// tcgen05.ld (one TMEM lane per output row).  The operand loaders differ per contraction (row or
+// column gathers of the same row-major buffers), so no transposed copies are made.  Every wait is
+// bounded: on expiry the kernel flags HGB_STATUS_ITERATION_LIMIT, frees its tensor memory and
+// returns.
+//
+// Dynamic shared memory per CTA is 100 KB, so at most two CTAs share an SM and their two 256-column
+// allocations always fit the SM's 512 TMEM columns (an allocation never waits).
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "hgb_common.cuh"
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int TM = 128;            // output rows per CTA (tcgen05 M)
+constexpr int KC = 64;             // reduction slice staged per round
+constexpr int NMAX = 256;          // output columns per CTA (tcgen05 N limit for M = 128)
+constexpr int THREADS = 128;
+constexpr int TMEM_COLS = 256;
+constexpr int SMEM_A = TM * KC * 2;        // 16 KB
+constexpr int SMEM_B = NMAX * KC * 2;      // 32 KB
+constexpr int SMEM_DYN = 100 * 1024;       // holds A + B; sized to cap residency at two CTAs per SM
+static_assert(SMEM_A + SMEM_B <= SMEM_DYN, "staged slices must fit the dynamic shared memory");
+constexpr uint64_t WAIT_NS = 1000000000ull;   // a wait for the tensor core gives up after 1 s
+constexpr int WIDTH = 256;                 // row stride (elements) of the hidden activation buffers
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of a staged slice (r < rows, k < 64) in the canonical layout
+__device__ __forceinline__ int slice_off(int r, int k) {
+    return ((((r >> 3) << 3) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
+}
+
+// shared-memory matrix descriptor: start address, leading (K) byte offset 128, stride (8-row group)
+// byte offset 1024, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// non-blocking test of the phase with the given parity
+__device__ __forceinline__ bool mbar_test(uint32_t mbar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for the phase with the given parity to complete, for at most WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    if (mbar_test(mbar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    while (!mbar_test(mbar, parity))
+        if (global_ns() - t0 > WAIT_NS) return false;
+    return true;
+}
+
+// 16 consecutive fp32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.0f / (1.0f + expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigmoidf_(z); }
+__device__ __forceinline__ float silu_grad(float z) {
+    const float s = sigmoidf_(z);
+    return s * (1.0f + z * (1.0f - s));
+}
+
+union Pack8 {
+    uint4 u;
+    bf16 h[8];
+};
+
+// ---- operand loaders and epilogues of the three contractions -------------------------------------
+// A loader: 8 consecutive reduction entries of output row r; B loader: the same for output column n.
+// Both return zeros outside the operands.
+
+struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
+    const bf16 *x;
+    long x_es;
+    int ldx;
+    const bf16 *w;
+    long w_es;
+    const float *bias;
+    long b_es;
+    int K, N, batch, act;
+    float *pre;        // fp32 pre-activations [b][ldp] (hidden layers; may be null)
+    long pre_es;
+    bf16 *y;           // bf16 activations [b][ldy] (hidden layers)
+    long y_es;
+    float *out;        // fp32 outputs [b][N] (last layer)
+    long out_es;
+    int ldp, ldy;
+
+    __device__ int red() const { return K; }
+    __device__ int ncols() const { return N; }
+    __device__ uint4 load_a(int e, int row, int k) const {
+        if (row >= batch || k >= K) return make_uint4(0, 0, 0, 0);
+        return *(const uint4 *)(x + e * x_es + (long)row * ldx + k);
+    }
+    __device__ uint4 load_b(int e, int n, int k) const {
+        if (n >= N || k >= K) return make_uint4(0, 0, 0, 0);
+        return *(const uint4 *)(w + e * w_es + (long)n * K + k);
+    }
+    __device__ void store(int e, int row, int n0, const float (&v)[16]) const {
+        if (row >= batch || n0 >= N) return;
+        const float *bb = bias + e * b_es + n0;
+        if (act) {
+            Pack8 p0, p1;
+            float z[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) z[i] = v[i] + bb[i];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                p0.h[i] = __float2bfloat16_rn(silu(z[i]));
+                p1.h[i] = __float2bfloat16_rn(silu(z[i + 8]));
+            }
+            uint4 *yd = (uint4 *)(y + e * y_es + (long)row * ldy + n0);
+            yd[0] = p0.u;
+            yd[1] = p1.u;
+            if (pre) {
+                float4 *pd = (float4 *)(pre + e * pre_es + (long)row * ldp + n0);
+#pragma unroll
+                for (int i = 0; i < 4; i++) pd[i] = make_float4(z[4 * i], z[4 * i + 1], z[4 * i + 2], z[4 * i + 3]);
+            }
+        } else {
+            float4 *od = (float4 *)(out + e * out_es + (long)row * N + n0);
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                od[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1], v[4 * i + 2] + bb[4 * i + 2],
+                                    v[4 * i + 3] + bb[4 * i + 3]);
+        }
+    }
+};
+
+struct DxOp {   // dZprev[b][k] = (sum_n dZ[b][n] W[n][k]) * silu'(Zprev[b][k])
+    const bf16 *dz;    // [b][WIDTH], reduction over its first N columns
+    long dz_es;
+    const bf16 *w;     // [N][K]
+    long w_es;
+    const float *pre;  // Zprev [b][WIDTH]
+    long pre_es;
+    bf16 *dzp;         // dZprev [b][WIDTH]
+    long dzp_es;
+    int K, N, batch;
+
+    __device__ int red() const { return N; }
+    __device__ int ncols() const { return K; }
+    __device__ uint4 load_a(int e, int row, int n) const {
+        if (row >= batch || n >= N) return make_uint4(0, 0, 0, 0);
+        return *(const uint4 *)(dz + e * dz_es + (long)row * WIDTH + n);
+    }
+    __device__ uint4 load_b(int e, int k, int n) const {
+        Pack8 p;
+        const bf16 *wp = w + e * w_es + k;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            p.h[j] = (k < K && n + j < N) ? wp[(long)(n + j) * K] : __float2bfloat16_rn(0.0f);
+        return p.u;
+    }
+    __device__ void store(int e, int row, int k0, const float (&v)[16]) const {
+        if (row >= batch || k0 >= K) return;
+        const float *zp = pre + e * pre_es + (long)row * WIDTH + k0;
+        Pack8 p0, p1;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            p0.h[i] = __float2bfloat16_rn(v[i] * silu_grad(zp[i]));
+            p1.h[i] = __float2bfloat16_rn(v[i + 8] * silu_grad(zp[i + 8]));
+        }
+        uint4 *d = (uint4 *)(dzp + e * dzp_es + (long)row * WIDTH + k0);
+        d[0] = p0.u;
+        d[1] = p1.u;
+    }
+};
+
+struct DwOp {   // part[s][n][k] = sum over this split's rows b of dZ[b][n] X[b][k]
+    const bf16 *dz;    // [b][WIDTH]
+    long dz_es;
+    const bf16 *x;     // layer input [b][ldx]
+    long x_es;
+    int ldx;
+    float *part;       // [E][S][N][K]
+    int K, N, batch, rows_per_split, nsplit;
+
+    __device__ int red() const { return rows_per_split; }
+    __device__ int ncols() const { return K; }
+    __device__ uint4 load_a(int e, int n, int r) const {   // r: row offset inside the split
+        Pack8 p;
+        const int b0 = blockIdx.y * rows_per_split + r;
+        const bf16 *d = dz + e * dz_es + n;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int b = b0 + j;
+            p.h[j] = (n < N && r + j < rows_per_split && b < batch) ? d[(long)b * WIDTH] : __float2bfloat16_rn(0.0f);
+        }
+        return p.u;
+    }
+    __device__ uint4 load_b(int e, int k, int r) const {
+        Pack8 p;
+        const int b0 = blockIdx.y * rows_per_split + r;
+        const bf16 *xp = x + e * x_es + k;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int b = b0 + j;
+            p.h[j] = (k < K && r + j < rows_per_split && b < batch) ? xp[(long)b * ldx] : __float2bfloat16_rn(0.0f);
+        }
+        return p.u;
+    }
+    __device__ void store(int e, int n, int k0, const float (&v)[16]) const {
+        if (n >= N || k0 >= K) return;
+        float4 *d = (float4 *)(part + (((long)e * nsplit + blockIdx.y) * N + n) * K + k0);
+#pragma unroll
+        for (int i = 0; i < 4; i++) d[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+    }
+};
+
+// One 128 x ncols output tile (blockIdx.x: row tile, blockIdx.z: ensemble member).
+template <class Op>
+__global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    uint8_t *sa = smem;
+    uint8_t *sb = smem + SMEM_A;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.z;
+    const int row0 = blockIdx.x * TM;
+    const int ncols = op.ncols(), red = op.red();
+    const int npad = (ncols + 15) & ~15;
+    const uint32_t mb = smem_u32(&mbar);
+
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), TMEM_COLS);
+    if (threadIdx.x == 0) mbar_init(mb, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = idesc_bf16(TM, npad);
+
+    bool ok = true;
+    uint32_t parity = 0;
+    const int nslices = (red + KC - 1) / KC;
+    for (int c = 0; c < nslices; c++) {
+        const int k0 = c * KC;
+        for (int v = threadIdx.x; v < TM * (KC / 8); v += THREADS) {
+            const int r = v % TM, kg = v / TM;
+            *(uint4 *)(sa + slice_off(r, kg * 8)) = op.load_a(e, row0 + r, k0 + kg * 8);
+        }
+        for (int v = threadIdx.x; v < npad * (KC / 8); v += THREADS) {
+            const int n = v % npad, kg = v / npad;
+            *(uint4 *)(sb + slice_off(n, kg * 8)) = op.load_b(e, n, k0 + kg * 8);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+            const int ksteps = min(KC, ((red - k0) + 15) & ~15) / 16;
+            for (int s = 0; s < ksteps; s++)
+                mma_bf16(tmem, smem_desc(smem_u32(sa) + 256 * s), smem_desc(smem_u32(sb) + 256 * s), idesc,
+                         (c > 0 || s > 0) ? 1u : 0u);
+            mma_commit(mb);
+        }
+        // every thread waits: the next slice overwrites shared memory, the epilogue reads TMEM
+        const bool done = mbar_wait(mb, parity);
+        parity ^= 1u;
+        if (!__syncthreads_and(done)) {
+            ok = false;
+            break;
+        }
+    }
+    tc_fence_after();
+    if (ok) {
+        const int m = warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int n0 = 0; n0 < npad; n0 += 16) {
+            float v[16];
+            tmem_ld16(lane_addr + (uint32_t)n0, v);
+            op.store(e, row0 + m, n0, v);
+        }
+    } else {
+        if (threadIdx.x == 0) hgb::flag(status, HGB_STATUS_ITERATION_LIMIT);
+        mbar_wait(mb, parity ^ 1u);   // give the tensor core a last bounded chance to finish
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+}
+
+// ---- loss, gradient reduction, optimiser ----------------------------------------------------------
+
+struct NetView {
+    int L, E;
+    int K[HGB_MLP_MAX_LAYERS], N[HGB_MLP_MAX_LAYERS];
+    long w_off[HGB_MLP_MAX_LAYERS], p_off[HGB_MLP_MAX_LAYERS], b_off[HGB_MLP_MAX_LAYERS];
+    long n_w, n_p;   // bf16 weights and fp32 parameters per member
+};
+
+NetView view_of(const hgb_mlp *net) {
+    NetView v{};
+    v.L = net->n_layers;
+    v.E = net->n_members;
+    long ow = 0, op = 0;
+    for (int l = 0; l < v.L; l++) {
+        v.K[l] = net->dims[l];
+        v.N[l] = net->dims[l + 1];
+        v.w_off[l] = ow;
+        v.p_off[l] = op;
+        v.b_off[l] = op + (long)v.N[l] * v.K[l];
+        ow += (long)v.N[l] * v.K[l];
+        op += (long)v.N[l] * v.K[l] + v.N[l];
+    }
+    v.n_w = ow;
+    v.n_p = op;
+    return v;
+}
+
+// loss[e] = mean (out - target)^2; dZ of the last layer = d loss / d out (bf16), one block per member
+__global__ void k_mse(int batch, int nout, const float *__restrict__ out, const float *__restrict__ target,
+                      long t_es, bf16 *__restrict__ dz, long dz_es, float *__restrict__ loss) {
+    const int e = blockIdx.x;
+    const float scale = 2.0f / ((float)batch * (float)nout);
+    float acc = 0.0f;
+    for (long i = threadIdx.x; i < (long)batch * nout; i += blockDim.x) {
+        const long b = i / nout, n = i % nout;
+        const float d = out[e * (long)batch * nout + i] - target[e * t_es + i];
+        acc += d * d;
+        dz[e * dz_es + b * WIDTH + n] = __float2bfloat16_rn(scale * d);
+    }
+    __shared__ float red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && loss) loss[e] = red[0] / ((float)batch * (float)nout);
+}
+
+struct GradArgs {
+    NetView v;
+    int batch, nsplit;
+    const float *part[HGB_MLP_MAX_LAYERS];   // [E][S][N][K]
+    const bf16 *dz[HGB_MLP_MAX_LAYERS];      // [E][B][WIDTH]
+    long dz_es;
+    float *grad;                             // [E][n_p]
+};
+
+// weight gradients: the split partials summed in split order; bias gradients: dZ summed over the batch
+__global__ void k_grad_reduce(GradArgs a) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)a.v.E * a.v.n_p) return;
+    const int e = (int)(idx / a.v.n_p);
+    const long p = idx % a.v.n_p;
+    int l = 0;
+    while (l + 1 < a.v.L && p >= a.v.p_off[l + 1]) l++;
+    const int K = a.v.K[l], N = a.v.N[l];
+    float g = 0.0f;
+    if (p < a.v.b_off[l]) {
+        const long wi = p - a.v.p_off[l];
+        const float *pp = a.part[l] + (long)e * a.nsplit * N * K + wi;
+        for (int s = 0; s < a.nsplit; s++) g += pp[(long)s * N * K];
+    } else {
+        const int n = (int)(p - a.v.b_off[l]);
+        const bf16 *d = a.dz[l] + e * a.dz_es + n;
+        for (int b = 0; b < a.batch; b++) g += __bfloat162float(d[(long)b * WIDTH]);
+    }
+    a.grad[idx] = g;
+}
+
+// decoupled AdamW on the fp32 master parameters; weights (not biases) decay; bf16 weight copies written
+__global__ void k_adamw(NetView v, float *__restrict__ params, const float *__restrict__ grad, float *__restrict__ m1,
+                        float *__restrict__ m2, bf16 *__restrict__ w, float lr, float b1, float b2, float eps, float wd,
+                        float bc1, float bc2) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)v.E * v.n_p) return;
+    const int e = (int)(idx / v.n_p);
+    const long p = idx % v.n_p;
+    int l = 0;
+    while (l + 1 < v.L && p >= v.p_off[l + 1]) l++;
+    const bool is_w = p < v.b_off[l];
+    const float g = grad[idx];
+    const float a = b1 * m1[idx] + (1.0f - b1) * g;
+    const float b = b2 * m2[idx] + (1.0f - b2) * g * g;
+    m1[idx] = a;
+    m2[idx] = b;
+    float x = params[idx];
+    if (is_w) x -= lr * wd * x;
+    x -= lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+    params[idx] = x;
+    if (is_w) w[(long)e * v.n_w + v.w_off[l] + (p - v.p_off[l])] = __float2bfloat16_rn(x);
+}
+
+__global__ void k_pack_weights(NetView v, const float *__restrict__ params, bf16 *__restrict__ w) {
+    const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long)v.E * v.n_p) return;
+    const int e = (int)(idx / v.n_p);
+    const long p = idx % v.n_p;
+    int l = 0;
+    while (l + 1 < v.L && p >= v.p_off[l + 1]) l++;
+    if (p < v.b_off[l]) w[(long)e * v.n_w + v.w_off[l] + (p - v.p_off[l])] = __float2bfloat16_rn(params[idx]);
+}
+
+int check_net(const hgb_mlp *net) {
+    if (!net || net->n_layers < 1 || net->n_layers > HGB_MLP_MAX_LAYERS || net->n_members < 1) return 0;
+    if (net->n_members > 65535) return 0;
+    for (int l = 0; l <= net->n_layers; l++) {
+        const int d = net->dims[l];
+        if (d < 16 || d > NMAX || (d & 15)) return 0;
+    }
+    return 1;
+}
+
+template <class Op>
+int launch_gemm(const Op &op, int row_tiles, int splits, int members, int *status, cudaStream_t st) {
+    static bool attr_set = false;   // idempotent; set before the first launch of each instantiation
+    if (!attr_set) {
+        cudaError_t err = cudaFuncSetAttribute(k_mlp_gemm<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+        attr_set = true;
+    }
+    dim3 grid((unsigned)row_tiles, (unsigned)splits, (unsigned)members);
+    k_mlp_gemm<Op><<<grid, THREADS, SMEM_DYN, st>>>(op, status);
+    return hgb::check_launch();
+}
+
+const float *param_bias(const hgb_mlp *net, const NetView &v, int l) { return net->params + v.b_off[l]; }
+
+}  // namespace
+
+extern "C" {
+
+long hgb_mlp_param_count(const hgb_mlp *net) { return check_net(net) ? view_of(net).n_p : -1; }
+
+long hgb_mlp_weight_count(const hgb_mlp *net) { return check_net(net) ? view_of(net).n_w : -1; }
+
+int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, uint16_t *act,
+                    float *pre, float *out, int *d_status, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && net->params && net->weights && x && act && out && batch >= 0);
+    HGB_CHECK_ARG(x_member_stride >= 0);
+    if (batch == 0) return HGB_OK;
+    const NetView v = view_of(net);
+    cudaStream_t st = (cudaStream_t)stream;
+    const long hid_es = (long)batch * WIDTH;            // member stride of one layer's hidden buffer
+    const long hid_ls = (long)v.E * hid_es;             // layer stride
+    const int tiles = (int)hgb::ceil_div(batch, TM);
+    for (int l = 0; l < v.L; l++) {
+        FwdOp op{};
+        const bool first = l == 0, last = l == v.L - 1;
+        op.x = first ? (const bf16 *)x : (const bf16 *)act + (l - 1) * hid_ls;
+        op.x_es = first ? x_member_stride : hid_es;
+        op.ldx = first ? v.K[0] : WIDTH;
+        op.w = (const bf16 *)net->weights + v.w_off[l];
+        op.w_es = v.n_w;
+        op.bias = param_bias(net, v, l);
+        op.b_es = v.n_p;
+        op.K = v.K[l];
+        op.N = v.N[l];
+        op.batch = batch;
+        op.act = last ? 0 : 1;
+        op.pre = (last || !pre) ? nullptr : pre + l * hid_ls;
+        op.pre_es = hid_es;
+        op.ldp = WIDTH;
+        op.y = last ? nullptr : (bf16 *)act + l * hid_ls;
+        op.y_es = hid_es;
+        op.ldy = WIDTH;
+        op.out = last ? out : nullptr;
+        op.out_es = (long)batch * v.N[l];
+        int rc = launch_gemm(op, tiles, 1, v.E, d_status, st);
+        if (rc) return rc;
+    }
+    return HGB_OK;
+}
+
+size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch) {
+    if (!check_net(net) || batch <= 0) return 0;
+    const NetView v = view_of(net);
+    const int nsplit = (int)hgb::ceil_div(batch, HGB_MLP_SPLIT_ROWS);
+    size_t bytes = sizeof(uint16_t) * (size_t)v.L * v.E * batch * WIDTH;   // dZ per layer
+    for (int l = 0; l < v.L; l++) bytes += sizeof(float) * (size_t)v.E * nsplit * v.N[l] * v.K[l];
+    return bytes;
+}
+
+int hgb_mlp_backward(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, const uint16_t *act,
+                     const float *pre, const float *out, const float *target, long target_member_stride, float *grad,
+                     float *loss, void *workspace, size_t workspace_bytes, int *d_status, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && net->params && net->weights && x && act && pre && out && target && grad);
+    HGB_CHECK_ARG(batch >= 1 && x_member_stride >= 0 && target_member_stride >= 0);
+    HGB_CHECK_ARG(workspace && workspace_bytes >= hgb_mlp_backward_workspace_bytes(net, batch));
+    const NetView v = view_of(net);
+    cudaStream_t st = (cudaStream_t)stream;
+    const long hid_es = (long)batch * WIDTH, hid_ls = (long)v.E * hid_es;
+    const int nsplit = (int)hgb::ceil_div(batch, HGB_MLP_SPLIT_ROWS);
+    bf16 *dz = (bf16 *)workspace;
+    float *part = (float *)((char *)workspace + sizeof(uint16_t) * (size_t)v.L * hid_ls);
+    GradArgs ga{};
+    ga.v = v;
+    ga.batch = batch;
+    ga.nsplit = nsplit;
+    ga.dz_es = hid_es;
+    ga.grad = grad;
+    {
+        float *pp = part;
+        for (int l = 0; l < v.L; l++) {
+            ga.part[l] = pp;
+            ga.dz[l] = dz + l * hid_ls;
+            pp += (size_t)v.E * nsplit * v.N[l] * v.K[l];
+        }
+    }
+    const int last = v.L - 1;
+    k_mse<<<v.E, 256, 0, st>>>(batch, v.N[last], out, target, target_member_stride, dz + last * hid_ls, hid_es, loss);
+    int rc = hgb::check_launch();
+    if (rc) return rc;
+    for (int l = last; l >= 0; l--) {
+        DwOp dw{};
+        dw.dz = dz + l * hid_ls;
+        dw.dz_es = hid_es;
+        dw.x = l == 0 ? (const bf16 *)x : (const bf16 *)act + (l - 1) * hid_ls;
+        dw.x_es = l == 0 ? x_member_stride : hid_es;
+        dw.ldx = l == 0 ? v.K[0] : WIDTH;
+        dw.part = const_cast<float *>(ga.part[l]);
+        dw.K = v.K[l];
+        dw.N = v.N[l];
+        dw.batch = batch;
+        dw.rows_per_split = HGB_MLP_SPLIT_ROWS;
+        dw.nsplit = nsplit;
+        if ((rc = launch_gemm(dw, (int)hgb::ceil_div(v.N[l], TM), nsplit, v.E, d_status, st))) return rc;
+        if (l == 0) break;
+        DxOp dx{};
+        dx.dz = dz + l * hid_ls;
+        dx.dz_es = hid_es;
+        dx.w = (const bf16 *)net->weights + v.w_off[l];
+        dx.w_es = v.n_w;
+        dx.pre = pre + (l - 1) * hid_ls;
+        dx.pre_es = hid_es;
+        dx.dzp = dz + (l - 1) * hid_ls;
+        dx.dzp_es = hid_es;
+        dx.K = v.K[l];
+        dx.N = v.N[l];
+        dx.batch = batch;
+        if ((rc = launch_gemm(dx, (int)hgb::ceil_div(batch, TM), 1, v.E, d_status, st))) return rc;
+    }
+    const long np = (long)v.E * v.n_p;
+    k_grad_reduce<<<(unsigned)hgb::ceil_div(np, 256), 256, 0, st>>>(ga);
+    return hgb::check_launch();
+}
+
+int hgb_mlp_adamw(const hgb_mlp *net, float *params, const float *grad, float *m1, float *m2, uint16_t *weights,
+                  int step, float lr, float beta1, float beta2, float eps, float weight_decay, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && params && grad && m1 && m2 && weights && step >= 1);
+    const NetView v = view_of(net);
+    const long np = (long)v.E * v.n_p;
+    const float bc1 = 1.0f - powf(beta1, (float)step), bc2 = 1.0f - powf(beta2, (float)step);
+    k_adamw<<<(unsigned)hgb::ceil_div(np, 256), 256, 0, (cudaStream_t)stream>>>(
+        v, params, grad, m1, m2, (bf16 *)weights, lr, beta1, beta2, eps, weight_decay, bc1, bc2);
+    return hgb::check_launch();
+}
+
+int hgb_mlp_pack_weights(const hgb_mlp *net, const float *params, uint16_t *weights, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && params && weights);
+    const NetView v = view_of(net);
+    const long np = (long)v.E * v.n_p;
+    k_pack_weights<<<(unsigned)hgb::ceil_div(np, 256), 256, 0, (cudaStream_t)stream>>>(v, params, (bf16 *)weights);
+    return hgb::check_launch();
+}
+
+}  // extern "C"

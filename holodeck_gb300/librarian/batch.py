@@ -83,9 +83,9 @@ def make_jobs(space, shapes=None, nreals=None, seed=0, indices=None):
     return jobs
 
 
-def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags):
-    """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: dict or None}
-    and {index: exception} for samples that failed."""
+def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=None):
+    """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: result or None}
+    and {index: exception} for samples that failed.  A result is run_model's dict, or ``reduce`` of it."""
     t = D.torch()
     dev = D.device()
     order = sorted(jobs, key=lambda j: -j.cost(nfreqs))
@@ -104,8 +104,9 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags):
                     return
                 try:
                     sam, hard = space.model_for_params(job.params, job.shape)
-                    results[job.index] = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
-                                                   nloudest=nloudest, seed=job.seed, **flags)
+                    res = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
+                                    nloudest=nloudest, seed=job.seed, **flags)
+                    results[job.index] = res if reduce is None else reduce(res)
                 except Exception as err:   # a failed sample gives NaN rows, as in the reference's libraries
                     results[job.index] = None
                     errors[job.index] = err
@@ -195,7 +196,7 @@ def autotune(space, jobs, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST, pta_du
 
 def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST,
                 pta_dur=DEF_PTA_DUR, seed=0, singles_flag=True, gwb_flag=False, params_flag=False,
-                details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None):
+                details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None, reduce=None):
     """Evaluate the samples of ``space`` (all, or ``indices``) on this GPU; returns the list of
     per-sample :func:`lib_tools.run_model` dicts in sample order (``None`` for a failed sample), the
     input that :func:`lib_tools.write_library` takes.
@@ -204,6 +205,8 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     keys every sample's realizations (:func:`sample_seed`).  ``workers`` / ``waves`` fix the
     schedule; otherwise it comes from :func:`autotune` (``tune=True``) or defaults to (3, 2).
     ``stats``, when a dict, receives the schedule, wall time, sample count, realizations and draws.
+    ``reduce``, when given, maps each sample's dict to what is kept (on the worker, as soon as the
+    sample is done), so large libraries need not hold every realization in host memory.
     """
     flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag)
     jobs = make_jobs(space, shapes, nreals, seed, indices)
@@ -224,7 +227,7 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     try:
         D.torch().cuda.synchronize()
         t0 = time.perf_counter()
-        results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags)
+        results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags, reduce)
         D.torch().cuda.synchronize()
         wall = time.perf_counter() - t0
     finally:

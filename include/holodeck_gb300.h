@@ -352,6 +352,46 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
                         int mode, uint64_t seed, const double *replay, double *gwb,
                         void *workspace, size_t workspace_bytes, int *d_status, void *stream);
 
+/* ---- Emulator MLP ensemble (no reference counterpart: the reference's emulators are Gaussian
+ * processes, holodeck/gps/gp_utils.py; this network is trained on libraries the GPU SAM writes).
+ * E members, each dims[0] -> dims[1] -> ... -> dims[n_layers] with SiLU after every layer but the
+ * last.  Every width is a multiple of 16 in [16, 256] (inputs are zero-padded to 16).  Per member
+ * the fp32 parameters are laid out layer by layer as W_l [dims[l+1]][dims[l]] (row-major) then
+ * b_l [dims[l+1]] (P values, hgb_mlp_param_count); `weights` holds bf16 copies of the W_l only
+ * (Pw values, hgb_mlp_weight_count), kept in step by hgb_mlp_adamw / hgb_mlp_pack_weights.
+ * bf16 buffers are passed as uint16_t bit patterns.  Hidden activations live in buffers with a row
+ * stride of 256: act and pre hold layers 0..n_layers-2 as [layer][member][batch][256] (bf16 and
+ * fp32), out is [member][batch][dims[n_layers]] fp32.  All products accumulate in fp32 on the
+ * tensor cores (tcgen05, accumulators in tensor memory). */
+#define HGB_MLP_MAX_LAYERS 8
+#define HGB_MLP_SPLIT_ROWS 128   /* batch rows per partial of a weight gradient */
+typedef struct {
+    int n_layers;
+    int n_members;
+    int dims[HGB_MLP_MAX_LAYERS + 1];
+    const float *params;       /* fp32 [E][P] */
+    const uint16_t *weights;   /* bf16 [E][Pw] */
+} hgb_mlp;
+
+long hgb_mlp_param_count(const hgb_mlp *net);    /* P, or -1 for an invalid description */
+long hgb_mlp_weight_count(const hgb_mlp *net);   /* Pw, or -1 */
+/* x: bf16 [batch][dims[0]] per member (x_member_stride elements apart; 0 = one input for all);
+ * pre may be NULL (inference). */
+int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, uint16_t *act,
+                    float *pre, float *out, int *d_status, void *stream);
+size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch);
+/* Mean-squared-error loss against target [batch][dims[n_layers]] (target_member_stride apart) of the
+ * outputs of the last hgb_mlp_forward (with pre): loss[e] (may be NULL) and grad [E][P] fp32. */
+int hgb_mlp_backward(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, const uint16_t *act,
+                     const float *pre, const float *out, const float *target, long target_member_stride,
+                     float *grad, float *loss, void *workspace, size_t workspace_bytes, int *d_status,
+                     void *stream);
+/* Decoupled AdamW step `step` (>= 1) on params [E][P] with moments m1, m2 [E][P]; weights, not
+ * biases, decay; writes the bf16 weight copies. */
+int hgb_mlp_adamw(const hgb_mlp *net, float *params, const float *grad, float *m1, float *m2, uint16_t *weights,
+                  int step, float lr, float beta1, float beta2, float eps, float weight_decay, void *stream);
+int hgb_mlp_pack_weights(const hgb_mlp *net, const float *params, uint16_t *weights, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
