@@ -499,6 +499,24 @@ def run_profile(args):
     print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1}))
 
 
+def run_mlp_profile(args):
+    """The emulator network's kernels at a fixed size, untimed (the program the MLP ncu captures run):
+    a 4-member 16 -> 4x256 -> 160 ensemble, one forward of 1024 queries, then one training step
+    (forward, backward, AdamW) on a batch of 512."""
+    import torch
+    from holodeck_gb300.emulator import MLPEnsemble
+    net = MLPEnsemble([16, 256, 256, 256, 256, 160], members=4, seed=0)
+    rng = np.random.default_rng(0)
+    x = torch.as_tensor(rng.uniform(-1, 1, size=(1024, 16)).astype(np.float32), device="cuda").to(torch.bfloat16)
+    for _ in range(args.warmup + 1):
+        net.forward(x)
+    t = torch.as_tensor(rng.normal(size=(512, 160)).astype(np.float32), device="cuda")
+    net.train_step(x[:512].contiguous(), t, lr=1e-3)
+    torch.cuda.synchronize()
+    net.check_status()
+    print(json.dumps({"profile": "emulator MLP 16-4x256-160, 4 members", "forward_batch": 1024, "train_batch": 512}))
+
+
 def run_stages(args):
     """Device time of each stage of one model evaluation (CUDA events on the current stream), median
     over ``--steps`` evaluations after ``--warmup``: the breakdown behind the headline number.  The
@@ -554,6 +572,7 @@ def main():
                     help="training samples of the emulator measurement carried by the bench line (0: skip)")
     ap.add_argument("--emulator-steps", type=int, default=6000, help="emulator training steps (batch 512)")
     ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
+    ap.add_argument("--mlp-profile", action="store_true", help="untimed emulator-network kernels (for ncu)")
     ap.add_argument("--emulator-cache", default=None,
                     help=".npz holding the emulator's training library statistics (written when absent)")
     args = ap.parse_args()
@@ -565,6 +584,8 @@ def main():
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps({"metric": METRIC, "emulator": run_emulator(args)}))
+    elif args.mlp_profile:
+        run_mlp_profile(args)
     elif args.profile:
         run_profile(args)
     elif args.stages:

@@ -9,19 +9,22 @@
 // accumulated in fp32.
 //
 // All three contractions (forward Y = X W^T, input gradient dX = dZ W, weight gradient
-// dW = dZ^T X) run on one tensor-core core: a CTA of 128 threads owns a 128-row output tile with up
-// to 256 columns in tensor memory (tcgen05.alloc, 256 columns of fp32), stages 64-wide slices of the
+// dW = dZ^T X) run on one tensor-core core: a CTA of 128 threads owns a 128-row output tile of NT
+// columns in tensor memory (tcgen05.alloc, fp32 accumulators), stages KC-wide slices of the
 // reduction axis of both operands in shared memory in the canonical no-swizzle K-major layout
-// (8 x 16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row groups 1024 B apart), and
-// one elected thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = 128, K = 16 per
+// (8 x 16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row groups 16 KC bytes apart),
+// and one elected thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = 128, K = 16 per
 // instruction) and commits them to an mbarrier; the epilogue reads the accumulator back with
-// tcgen05.ld (one TMEM lane per output row).  The operand loaders differ per contraction (row or
-// column gathers of the same row-major buffers), so no transposed copies are made.  Every wait is
-// bounded: on expiry the kernel flags HGB_STATUS_ITERATION_LIMIT, frees its tensor memory and
-// returns.
+// tcgen05.ld (one TMEM lane per output row).  The forward and input-gradient contractions stage the
+// whole reduction axis (<= 256) at once and split the output columns 64 per CTA, so a layer is one
+// load / MMA / read-back round trip on (row tiles x column tiles x members) CTAs, which is what keeps
+// a single-query forward short; the weight gradient keeps all columns in one CTA and stages one
+// 128-row batch split per CTA.  The operand loaders differ per contraction (row or column gathers of
+// the same row-major buffers), so no transposed copies are made.  Every wait is bounded: on expiry
+// the kernel flags HGB_STATUS_ITERATION_LIMIT, frees its tensor memory and returns.
 //
-// Dynamic shared memory per CTA is 100 KB, so at most two CTAs share an SM and their two 256-column
-// allocations always fit the SM's 512 TMEM columns (an allocation never waits).
+// Dynamic shared memory per CTA is 100 KB, so at most two CTAs share an SM and their allocations
+// (at most 256 columns each) always fit the SM's 512 TMEM columns (an allocation never waits).
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
@@ -33,28 +36,24 @@ namespace {
 typedef __nv_bfloat16 bf16;
 
 constexpr int TM = 128;            // output rows per CTA (tcgen05 M)
-constexpr int KC = 64;             // reduction slice staged per round
-constexpr int NMAX = 256;          // output columns per CTA (tcgen05 N limit for M = 128)
+constexpr int NMAX = 256;          // widest layer (tcgen05 N limit for M = 128)
 constexpr int THREADS = 128;
-constexpr int TMEM_COLS = 256;
-constexpr int SMEM_A = TM * KC * 2;        // 16 KB
-constexpr int SMEM_B = NMAX * KC * 2;      // 32 KB
-constexpr int SMEM_DYN = 100 * 1024;       // holds A + B; sized to cap residency at two CTAs per SM
-static_assert(SMEM_A + SMEM_B <= SMEM_DYN, "staged slices must fit the dynamic shared memory");
+constexpr int SMEM_DYN = 100 * 1024;       // holds both staged slices; caps residency at two CTAs per SM
 constexpr uint64_t WAIT_NS = 1000000000ull;   // a wait for the tensor core gives up after 1 s
 constexpr int WIDTH = 256;                 // row stride (elements) of the hidden activation buffers
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// byte offset of element (r, k) of a staged slice (r < rows, k < 64) in the canonical layout
+// byte offset of element (r, k) of a staged slice (k < KC) in the canonical layout
+template <int KC>
 __device__ __forceinline__ int slice_off(int r, int k) {
-    return ((((r >> 3) << 3) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
+    return (((r >> 3) * (KC / 8) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
 // shared-memory matrix descriptor: start address, leading (K) byte offset 128, stride (8-row group)
-// byte offset 1024, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+// byte offset `sbo`, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
            (1ull << 46);
 }
 
@@ -150,6 +149,8 @@ union Pack8 {
 // Both return zeros outside the operands.
 
 struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
+    static constexpr int KC = 256, NT = 64;
+    static constexpr bool COL_TILED = true;
     const bf16 *x;
     long x_es;
     int ldx;
@@ -167,7 +168,7 @@ struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
     int ldp, ldy;
 
     __device__ int red() const { return K; }
-    __device__ int ncols() const { return N; }
+    __host__ __device__ int ncols() const { return N; }
     __device__ uint4 load_a(int e, int row, int k) const {
         if (row >= batch || k >= K) return make_uint4(0, 0, 0, 0);
         return *(const uint4 *)(x + e * x_es + (long)row * ldx + k);
@@ -208,6 +209,8 @@ struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
 };
 
 struct DxOp {   // dZprev[b][k] = (sum_n dZ[b][n] W[n][k]) * silu'(Zprev[b][k])
+    static constexpr int KC = 256, NT = 64;
+    static constexpr bool COL_TILED = true;
     const bf16 *dz;    // [b][WIDTH], reduction over its first N columns
     long dz_es;
     const bf16 *w;     // [N][K]
@@ -219,7 +222,7 @@ struct DxOp {   // dZprev[b][k] = (sum_n dZ[b][n] W[n][k]) * silu'(Zprev[b][k])
     int K, N, batch;
 
     __device__ int red() const { return N; }
-    __device__ int ncols() const { return K; }
+    __host__ __device__ int ncols() const { return K; }
     __device__ uint4 load_a(int e, int row, int n) const {
         if (row >= batch || n >= N) return make_uint4(0, 0, 0, 0);
         return *(const uint4 *)(dz + e * dz_es + (long)row * WIDTH + n);
@@ -248,6 +251,8 @@ struct DxOp {   // dZprev[b][k] = (sum_n dZ[b][n] W[n][k]) * silu'(Zprev[b][k])
 };
 
 struct DwOp {   // part[s][n][k] = sum over this split's rows b of dZ[b][n] X[b][k]
+    static constexpr int KC = HGB_MLP_SPLIT_ROWS, NT = NMAX;
+    static constexpr bool COL_TILED = false;   // blockIdx.y is the batch split
     const bf16 *dz;    // [b][WIDTH]
     long dz_es;
     const bf16 *x;     // layer input [b][ldx]
@@ -257,7 +262,7 @@ struct DwOp {   // part[s][n][k] = sum over this split's rows b of dZ[b][n] X[b]
     int K, N, batch, rows_per_split, nsplit;
 
     __device__ int red() const { return rows_per_split; }
-    __device__ int ncols() const { return K; }
+    __host__ __device__ int ncols() const { return K; }
     __device__ uint4 load_a(int e, int n, int r) const {   // r: row offset inside the split
         Pack8 p;
         const int b0 = blockIdx.y * rows_per_split + r;
@@ -288,9 +293,17 @@ struct DwOp {   // part[s][n][k] = sum over this split's rows b of dZ[b][n] X[b]
     }
 };
 
-// One 128 x ncols output tile (blockIdx.x: row tile, blockIdx.z: ensemble member).
+template <int N>
+__host__ __device__ constexpr int tmem_cols() { return N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256; }
+
+// One 128 x NT output tile (blockIdx.x: row tile, blockIdx.y: column tile or batch split,
+// blockIdx.z: ensemble member).
 template <class Op>
 __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
+    constexpr int KC = Op::KC, NT = Op::NT, COLS = tmem_cols<NT>();
+    constexpr int SMEM_A = TM * KC * 2;
+    static_assert(SMEM_A + NT * KC * 2 <= SMEM_DYN, "staged slices must fit the dynamic shared memory");
+    static_assert(KC % 16 == 0 && NT % 16 == 0 && NT <= NMAX, "tile shape");
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
@@ -299,11 +312,12 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int e = blockIdx.z;
     const int row0 = blockIdx.x * TM;
-    const int ncols = op.ncols(), red = op.red();
+    const int col0 = Op::COL_TILED ? (int)blockIdx.y * NT : 0;
+    const int ncols = min(NT, op.ncols() - col0), red = op.red();
     const int npad = (ncols + 15) & ~15;
     const uint32_t mb = smem_u32(&mbar);
 
-    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), TMEM_COLS);
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), COLS);
     if (threadIdx.x == 0) mbar_init(mb, 1);
     tc_fence_before();
     __syncthreads();
@@ -316,22 +330,22 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
     const int nslices = (red + KC - 1) / KC;
     for (int c = 0; c < nslices; c++) {
         const int k0 = c * KC;
-        for (int v = threadIdx.x; v < TM * (KC / 8); v += THREADS) {
+        const int kact = min(KC, ((red - k0) + 15) & ~15);   // staged (and multiplied) part of the slice
+        for (int v = threadIdx.x; v < TM * (kact / 8); v += THREADS) {
             const int r = v % TM, kg = v / TM;
-            *(uint4 *)(sa + slice_off(r, kg * 8)) = op.load_a(e, row0 + r, k0 + kg * 8);
+            *(uint4 *)(sa + slice_off<KC>(r, kg * 8)) = op.load_a(e, row0 + r, k0 + kg * 8);
         }
-        for (int v = threadIdx.x; v < npad * (KC / 8); v += THREADS) {
+        for (int v = threadIdx.x; v < npad * (kact / 8); v += THREADS) {
             const int n = v % npad, kg = v / npad;
-            *(uint4 *)(sb + slice_off(n, kg * 8)) = op.load_b(e, n, k0 + kg * 8);
+            *(uint4 *)(sb + slice_off<KC>(n, kg * 8)) = op.load_b(e, col0 + n, k0 + kg * 8);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (threadIdx.x == 0) {
             tc_fence_after();
-            const int ksteps = min(KC, ((red - k0) + 15) & ~15) / 16;
-            for (int s = 0; s < ksteps; s++)
-                mma_bf16(tmem, smem_desc(smem_u32(sa) + 256 * s), smem_desc(smem_u32(sb) + 256 * s), idesc,
-                         (c > 0 || s > 0) ? 1u : 0u);
+            for (int s = 0; s < kact / 16; s++)
+                mma_bf16(tmem, smem_desc(smem_u32(sa) + 256 * s, 16 * KC), smem_desc(smem_u32(sb) + 256 * s, 16 * KC),
+                         idesc, (c > 0 || s > 0) ? 1u : 0u);
             mma_commit(mb);
         }
         // every thread waits: the next slice overwrites shared memory, the epilogue reads TMEM
@@ -349,7 +363,7 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
         for (int n0 = 0; n0 < npad; n0 += 16) {
             float v[16];
             tmem_ld16(lane_addr + (uint32_t)n0, v);
-            op.store(e, row0 + m, n0, v);
+            op.store(e, row0 + m, col0 + n0, v);
         }
     } else {
         if (threadIdx.x == 0) hgb::flag(status, HGB_STATUS_ITERATION_LIMIT);
@@ -357,7 +371,7 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
+    if (warp == 0) tmem_dealloc(tmem, COLS);
 }
 
 // ---- loss, gradient reduction, optimiser ----------------------------------------------------------
@@ -485,7 +499,7 @@ int check_net(const hgb_mlp *net) {
 }
 
 template <class Op>
-int launch_gemm(const Op &op, int row_tiles, int splits, int members, int *status, cudaStream_t st) {
+int launch_gemm(const Op &op, int row_tiles, int members, int *status, cudaStream_t st, int splits = 1) {
     static bool attr_set = false;   // idempotent; set before the first launch of each instantiation
     if (!attr_set) {
         cudaError_t err = cudaFuncSetAttribute(k_mlp_gemm<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
@@ -495,7 +509,8 @@ int launch_gemm(const Op &op, int row_tiles, int splits, int members, int *statu
         }
         attr_set = true;
     }
-    dim3 grid((unsigned)row_tiles, (unsigned)splits, (unsigned)members);
+    const int ytiles = Op::COL_TILED ? (int)hgb::ceil_div(op.ncols(), Op::NT) : splits;
+    dim3 grid((unsigned)row_tiles, (unsigned)ytiles, (unsigned)members);
     k_mlp_gemm<Op><<<grid, THREADS, SMEM_DYN, st>>>(op, status);
     return hgb::check_launch();
 }
@@ -542,7 +557,7 @@ int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride,
         op.ldy = WIDTH;
         op.out = last ? out : nullptr;
         op.out_es = (long)batch * v.N[l];
-        int rc = launch_gemm(op, tiles, 1, v.E, d_status, st);
+        int rc = launch_gemm(op, tiles, v.E, d_status, st);
         if (rc) return rc;
     }
     return HGB_OK;
@@ -600,7 +615,7 @@ int hgb_mlp_backward(const hgb_mlp *net, const uint16_t *x, long x_member_stride
         dw.batch = batch;
         dw.rows_per_split = HGB_MLP_SPLIT_ROWS;
         dw.nsplit = nsplit;
-        if ((rc = launch_gemm(dw, (int)hgb::ceil_div(v.N[l], TM), nsplit, v.E, d_status, st))) return rc;
+        if ((rc = launch_gemm(dw, (int)hgb::ceil_div(v.N[l], TM), v.E, d_status, st, nsplit))) return rc;
         if (l == 0) break;
         DxOp dx{};
         dx.dz = dz + l * hid_ls;
@@ -614,7 +629,7 @@ int hgb_mlp_backward(const hgb_mlp *net, const uint16_t *x, long x_member_stride
         dx.K = v.K[l];
         dx.N = v.N[l];
         dx.batch = batch;
-        if ((rc = launch_gemm(dx, (int)hgb::ceil_div(batch, TM), 1, v.E, d_status, st))) return rc;
+        if ((rc = launch_gemm(dx, (int)hgb::ceil_div(batch, TM), v.E, d_status, st))) return rc;
     }
     const long np = (long)v.E * v.n_p;
     k_grad_reduce<<<(unsigned)hgb::ceil_div(np, 256), 256, 0, st>>>(ga);

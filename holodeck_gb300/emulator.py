@@ -292,8 +292,10 @@ class _GraphedForward:
         self.batch = int(batch)
         dev = emu.net.device
         self.h_in = t.zeros((self.batch, INPUT_PAD), dtype=t.bfloat16).pin_memory()
+        self.h_in_bits = self.h_in.view(t.int16).numpy()       # zero-copy view of the pinned inputs
         self.d_in = t.zeros((self.batch, INPUT_PAD), dtype=t.bfloat16, device=dev)
         self.h_out = t.zeros((emu.net.members, self.batch, emu.n_pad), dtype=t.float32).pin_memory()
+        self.h_out_np = self.h_out.numpy()
         self.stream = t.cuda.Stream(device=dev)
         with t.cuda.stream(self.stream):
             emu.net.forward(self.d_in)      # eager pass: lazy kernel attributes, buffers
@@ -308,16 +310,17 @@ class _GraphedForward:
     def __call__(self, params):
         t = D.torch()
         u = self.emu.unit(params)
-        q = u.shape[0]
+        q, npar = u.shape
         if q > self.batch:
             raise ValueError(f"at most {self.batch} queries per call")
-        x = np.zeros((self.batch, INPUT_PAD), dtype=np.float32)
-        x[:q, :u.shape[1]] = 2.0 * u - 1.0
-        self.h_in.copy_(t.as_tensor(x).to(t.bfloat16))
+        x = (2.0 * u - 1.0).astype(np.float32)
+        bits = x.view(np.uint32)
+        # round to the nearest bfloat16, ties to even (the conversion the eager path makes on the device)
+        self.h_in_bits[:q, :npar] = ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16).view(np.int16)
         with t.cuda.stream(self.stream):
             self.graph.replay()
         self.stream.synchronize()
-        out = self.h_out[:, :q, :self.emu.n_out].numpy().astype(np.float64) * self.emu.sd + self.emu.mu
+        out = self.h_out_np[:, :q, :self.emu.n_out].astype(np.float64) * self.emu.sd + self.emu.mu
         return out.mean(axis=0).reshape(q, self.emu.nfreqs, 4)
 
 
