@@ -298,7 +298,8 @@ def run_batched(args, rank=0, world=1):
     d2h = sum(sum(v.nbytes for k, v in r.items() if isinstance(v, np.ndarray)) for r in out if r is not None)
     tuning = stats.get("tuning") or {}
     table = tuning.get("table", {})
-    one = table.get(f"1,{stats['waves']}")
+    ones = [v for k, v in table.items() if k.split(",")[0] == "1"]
+    one = max(ones) if ones else None
     best = table.get(f"{stats['workers']},{stats['waves']}")
     return {"workload": BATCH_CONFIG, "samples": n, "failed": stats["failed"], "seconds": wall,
             "value": reals / wall, "unit": UNIT, "samples_per_s": n / wall, "draws_per_s": draws / wall,
