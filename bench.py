@@ -18,6 +18,7 @@ its held-out accuracy and query time against the plain GPU SAM's time for the sa
     python bench.py --stages        # per-stage device times
     python bench.py --batched       # only the batched-library measurement
     python bench.py --emulator [--emulator-samples 20000]   # only the emulator measurement
+    python bench.py --highres --steps 2   # the 181x161x201, 100-frequency, 10^4-realization workload
     python bench.py --profile --nfreqs K   # one untimed evaluation (the program ncu captures)
 
 --impl reference times the CPU restatement of the reference path (the oracle) on the host cores.
@@ -500,6 +501,64 @@ def run_profile(args):
     print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1}))
 
 
+HIRES_SHAPE = (181, 161, 201)
+HIRES_NFREQ, HIRES_NREALS = 100, 10000
+
+
+def run_highres(args):
+    """The high-resolution workload: 181 x 161 x 201 grid, 100 harmonics of 1/(16 yr), 10^4
+    realizations, 10 loudest (about 5.8e12 draws per evaluation), one untimed and ``--steps`` timed
+    evaluations (device-resident results), and the check of the realization mean of the total
+    characteristic strain against its FP64 expectation sum_b number_b h2fdf_b per frequency (the
+    z-score with the Poisson variance sum_b number_b h2fdf_b^2)."""
+    import torch
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    gsmf = H.sams.GSMF_Schechter(phi0=-2.77, mchar0_log10=11.24, alpha0=-1.24)
+    mmb = H.host_relations.MMBulge_KH2013(mamp_log10=8.69, mplaw=1.17, scatter_dex=0.28)
+    _, fe = H.utils.pta_freqs(16.0 * C.YR, HIRES_NFREQ)
+
+    def model():
+        sam = H.sams.Semi_Analytic_Model(shape=HIRES_SHAPE, gsmf=gsmf, gpf=H.sams.GPF_Power_Law(),
+                                         gmt=H.sams.GMT_Power_Law(), mmbulge=mmb)
+        hard = H.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * C.GYR, sepa_init=1.0e3 * C.PC, rchar=100.0 * C.PC,
+                                              gamma_inner=-1.0, gamma_outer=2.5)
+        return sam, hard
+
+    sam, hard = model()
+    sam.gwb(fe, hard=hard, realize=HIRES_NREALS, loudest=NLOUD, seed=1, return_torch=True)
+    times = []
+    for i in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        sam, hard = model()
+        ss, bg = sam.gwb(fe, hard=hard, realize=HIRES_NREALS, loudest=NLOUD, seed=2 + i, return_torch=True)
+        t1.record()
+        torch.cuda.synchronize()
+        times.append(t0.elapsed_time(t1) / 1e3)
+    redz_final, diff_num = sam._dbn_device(hard, H.utils.midpoints(fe) / 2.0)
+    number, h2fdf = sam._number_and_strain(fe / 2.0, diff_num, redz_final)
+    del redz_final, diff_num
+    lam, h = number.reshape(-1, HIRES_NFREQ), h2fdf.reshape(-1, HIRES_NFREQ)
+    s1 = (lam * h).sum(0).cpu().numpy()
+    s2 = (lam * h * h).sum(0).cpu().numpy()
+    nb = int(lam.shape[0])
+    del number, h2fdf, lam, h
+    total = (bg ** 2 + (ss ** 2).sum(-1)).cpu().numpy()
+    z = (total.mean(1) - s1) / np.sqrt(s2 / HIRES_NREALS)
+    sec = statistics.median(times)
+    return {"workload": (f"high-resolution plain SAM: grid {HIRES_SHAPE[0]}x{HIRES_SHAPE[1]}x{HIRES_SHAPE[2]}, "
+                         f"{HIRES_NFREQ} harmonics of 1/(16 yr), {HIRES_NREALS} realizations, {NLOUD} loudest"),
+            "value": HIRES_NREALS / sec, "unit": UNIT, "seconds_per_evaluation": sec, "evaluations": len(times),
+            "draws_per_s": nb * HIRES_NFREQ * HIRES_NREALS / sec,
+            "peak_device_memory_gb": torch.cuda.max_memory_allocated() / 1e9,
+            "mean_total_hc2_vs_expectation": {"z_min": float(z.min()), "z_median": float(np.median(z)),
+                                              "z_max": float(z.max()),
+                                              "rel_median": float(np.median(np.abs(total.mean(1) / s1 - 1.0)))}}
+
+
 def run_mlp_profile(args):
     """The emulator network's kernels at a fixed size, untimed (the program the MLP ncu captures run):
     a 4-member 16 -> 4x256 -> 160 ensemble, one forward of 1024 queries, then one training step
@@ -574,6 +633,8 @@ def main():
     ap.add_argument("--emulator-steps", type=int, default=6000, help="emulator training steps (batch 512)")
     ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
     ap.add_argument("--mlp-profile", action="store_true", help="untimed emulator-network kernels (for ncu)")
+    ap.add_argument("--highres", action="store_true",
+                    help="only the high-resolution workload (181x161x201, 100 frequencies, 10^4 realizations)")
     ap.add_argument("--emulator-cache", default=None,
                     help=".npz holding the emulator's training library statistics (written when absent)")
     args = ap.parse_args()
@@ -585,6 +646,10 @@ def main():
         import torch
         torch.cuda.set_device(dist_env()[2])
         print(json.dumps({"metric": METRIC, "emulator": run_emulator(args)}))
+    elif args.highres:
+        import torch
+        torch.cuda.set_device(dist_env()[2])
+        print(json.dumps({"metric": METRIC, "highres": run_highres(args)}))
     elif args.mlp_profile:
         run_mlp_profile(args)
     elif args.profile:
