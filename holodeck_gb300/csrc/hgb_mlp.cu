@@ -9,25 +9,32 @@
 // accumulated in fp32.
 //
 // All three contractions (forward Y = X W^T, input gradient dX = dZ W, weight gradient
-// dW = dZ^T X) run on one tensor-core core: a CTA of 128 threads owns a 128-row output tile of NT
-// columns in tensor memory (tcgen05.alloc, fp32 accumulators), stages KC-wide slices of the
-// reduction axis of both operands in shared memory in the canonical no-swizzle K-major layout
-// (8 x 16-byte core matrices, K-adjacent core matrices 128 B apart, 8-row groups 16 KC bytes apart),
-// and one elected thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = 128, K = 16 per
-// instruction) and commits them to an mbarrier; the epilogue reads the accumulator back with
-// tcgen05.ld (one TMEM lane per output row).  The forward and input-gradient contractions stage the
-// whole reduction axis (<= 256) at once and split the output columns 64 per CTA, so a layer is one
-// load / MMA / read-back round trip on (row tiles x column tiles x members) CTAs, which is what keeps
-// a single-query forward short; the weight gradient keeps all columns in one CTA and stages one
-// 128-row batch split per CTA.  The operand loaders differ per contraction (row or column gathers of
-// the same row-major buffers), so no transposed copies are made.  Every wait is bounded: on expiry
-// the kernel flags HGB_STATUS_ITERATION_LIMIT, frees its tensor memory and returns.
+// dW = dZ^T X) run on the tensor cores the same way: a CTA of 128 threads owns a 128-row output tile
+// of NT columns in tensor memory (tcgen05.alloc, fp32 accumulators), stages the operands in shared
+// memory in the canonical no-swizzle K-major layout (8 x 16-byte core matrices), one elected thread
+// issues tcgen05.mma (kind::f16, bf16 x bf16 -> fp32, M = 128, K = 16 per instruction) and commits
+// them to an mbarrier, and the epilogue reads the accumulator back with tcgen05.ld (one TMEM lane per
+// output row) and fuses bias, activation or the activation's derivative.
+//   * Forward (k_mlp_fwd_tma): both operands are row-major tiles, staged by the tensor memory
+//     accelerator (cp.async.bulk.tensor, one box of 8 columns per K-group) against an mbarrier;
+//     the whole reduction axis (<= 256) at once, output columns split 64 per CTA, so a layer is one
+//     copy / MMA / read-back round trip on (row tiles x column tiles x members) CTAs.
+//   * Input and weight gradients (k_mlp_gemm<DxOp / DwOp>): one operand is read transposed (a column
+//     gather of a row-major buffer), so the threads stage both operands through registers; the input
+//     gradient stages the whole reduction axis with columns split 64 per CTA, the weight gradient
+//     keeps all columns in one CTA and reduces one 128-row batch split per CTA.
+// Every wait is bounded: on expiry the kernel flags HGB_STATUS_ITERATION_LIMIT, frees its tensor
+// memory and returns.
 //
 // Dynamic shared memory per CTA is 100 KB, so at most two CTAs share an SM and their allocations
 // (at most 256 columns each) always fit the SM's 512 TMEM columns (an allocation never waits).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
+
+#include <mutex>
 
 #include "hgb_common.cuh"
 
@@ -50,11 +57,11 @@ __device__ __forceinline__ int slice_off(int r, int k) {
     return (((r >> 3) * (KC / 8) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1);
 }
 
-// shared-memory matrix descriptor: start address, leading (K) byte offset 128, stride (8-row group)
-// byte offset `sbo`, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t sbo) {
-    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
-           (1ull << 46);
+// shared-memory matrix descriptor: start address, leading byte offset `lbo` (next core matrix along
+// K), stride byte offset `sbo` (next 8-row group), descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
 // instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both K-major, M x N
@@ -144,13 +151,11 @@ union Pack8 {
     bf16 h[8];
 };
 
-// ---- operand loaders and epilogues of the three contractions -------------------------------------
+// ---- epilogues of the three contractions and the gradients' operand loaders -------------------------
 // A loader: 8 consecutive reduction entries of output row r; B loader: the same for output column n.
 // Both return zeros outside the operands.
 
-struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
-    static constexpr int KC = 256, NT = 64;
-    static constexpr bool COL_TILED = true;
+struct FwdOp {   // epilogue of the forward: Y[b][n] = act(acc + bias[n]) (operands staged by TMA)
     const bf16 *x;
     long x_es;
     int ldx;
@@ -167,16 +172,6 @@ struct FwdOp {   // Y[b][n] = act(sum_k X[b][k] W[n][k] + bias[n])
     long out_es;
     int ldp, ldy;
 
-    __device__ int red() const { return K; }
-    __host__ __device__ int ncols() const { return N; }
-    __device__ uint4 load_a(int e, int row, int k) const {
-        if (row >= batch || k >= K) return make_uint4(0, 0, 0, 0);
-        return *(const uint4 *)(x + e * x_es + (long)row * ldx + k);
-    }
-    __device__ uint4 load_b(int e, int n, int k) const {
-        if (n >= N || k >= K) return make_uint4(0, 0, 0, 0);
-        return *(const uint4 *)(w + e * w_es + (long)n * K + k);
-    }
     __device__ void store(int e, int row, int n0, const float (&v)[16]) const {
         if (row >= batch || n0 >= N) return;
         const float *bb = bias + e * b_es + n0;
@@ -304,7 +299,7 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
     constexpr int SMEM_A = TM * KC * 2;
     static_assert(SMEM_A + NT * KC * 2 <= SMEM_DYN, "staged slices must fit the dynamic shared memory");
     static_assert(KC % 16 == 0 && NT % 16 == 0 && NT <= NMAX, "tile shape");
-    extern __shared__ __align__(128) uint8_t smem[];
+    extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_slot;
     uint8_t *sa = smem;
@@ -344,8 +339,8 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
         if (threadIdx.x == 0) {
             tc_fence_after();
             for (int s = 0; s < kact / 16; s++)
-                mma_bf16(tmem, smem_desc(smem_u32(sa) + 256 * s, 16 * KC), smem_desc(smem_u32(sb) + 256 * s, 16 * KC),
-                         idesc, (c > 0 || s > 0) ? 1u : 0u);
+                mma_bf16(tmem, smem_desc(smem_u32(sa) + 256 * s, 128, 16 * KC),
+                         smem_desc(smem_u32(sb) + 256 * s, 128, 16 * KC), idesc, (c > 0 || s > 0) ? 1u : 0u);
             mma_commit(mb);
         }
         // every thread waits: the next slice overwrites shared memory, the epilogue reads TMEM
@@ -372,6 +367,151 @@ __global__ void __launch_bounds__(THREADS) k_mlp_gemm(Op op, int *status) {
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, COLS);
+}
+
+// ---- forward with TMA operand staging ----------------------------------------------------------------
+// The forward's operands are plain row-major tiles (activations [b][k], weights [n][k]), so the tensor
+// memory accelerator stages them: a box of 8 columns x R rows lands in shared memory as R rows of
+// 16 bytes, which is one K-group of core matrices for all R rows (8-row groups 128 B apart).  Stacking
+// the K-groups gives the canonical K-major layout with leading byte offset 16 R and stride byte
+// offset 128.  One thread issues every copy against one mbarrier (expect_tx of the boxes' bytes;
+// out-of-range rows and columns arrive as zeros), then the MMAs against the same barrier's next phase.
+
+constexpr int FWD_NT = 64;   // output columns per CTA
+constexpr int FWD_KMAX = 256;
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(mbar)
+        : "memory");
+}
+
+// blockIdx.x: 128-row tile, blockIdx.y: 64-column tile, blockIdx.z: member.  xmap: [members or 1][rows][K]
+// activations (x_member != 0 when each member has its own), wmap: [members][N][K] weights.
+__global__ void __launch_bounds__(THREADS) k_mlp_fwd_tma(const __grid_constant__ CUtensorMap xmap,
+                                                         const __grid_constant__ CUtensorMap wmap, FwdOp op,
+                                                         int x_member, int *status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    constexpr int COLS = tmem_cols<FWD_NT>();
+    uint8_t *sa = smem;                          // K/8 groups of 128 rows x 16 B
+    uint8_t *sb = smem + TM * FWD_KMAX * 2;      // K/8 groups of 64 rows x 16 B
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.z, row0 = blockIdx.x * TM, col0 = blockIdx.y * FWD_NT;
+    const int ncols = min(FWD_NT, op.N - col0);
+    const int groups = op.K / 8;
+    const uint32_t mb = smem_u32(&mbar);
+
+    if (warp == 0) tmem_alloc(smem_u32(&tmem_slot), COLS);
+    if (threadIdx.x == 0) mbar_init(mb, 1);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(mb, (uint32_t)groups * (TM + FWD_NT) * 16);
+        for (int g = 0; g < groups; g++) {
+            tma_load_3d(smem_u32(sa + g * TM * 16), &xmap, g * 8, row0, x_member ? e : 0, mb);
+            tma_load_3d(smem_u32(sb + g * FWD_NT * 16), &wmap, g * 8, col0, e, mb);
+        }
+    }
+    bool ok = __syncthreads_and(mbar_wait(mb, 0));
+    uint32_t pending = 0;   // parity of a phase still to complete when a wait gives up
+    if (ok) {
+        if (threadIdx.x == 0) {
+            tc_fence_after();
+            const uint32_t idesc = idesc_bf16(TM, ncols);
+            for (int s = 0; s < op.K / 16; s++)
+                mma_bf16(tmem, smem_desc(smem_u32(sa) + 2 * TM * 16 * s, TM * 16, 128),
+                         smem_desc(smem_u32(sb) + 2 * FWD_NT * 16 * s, FWD_NT * 16, 128), idesc, s > 0 ? 1u : 0u);
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, 1));
+        pending = 1;
+    }
+    tc_fence_after();
+    if (ok) {
+        const int m = warp * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int n0 = 0; n0 < ncols; n0 += 16) {
+            float v[16];
+            tmem_ld16(lane_addr + (uint32_t)n0, v);
+            op.store(e, row0 + m, col0 + n0, v);
+        }
+    } else {
+        if (threadIdx.x == 0) hgb::flag(status, HGB_STATUS_ITERATION_LIMIT);
+        mbar_wait(mb, pending);   // a last bounded wait for the copies or MMAs in flight
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, COLS);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+// bf16 tensor [d2][d1][d0] (d0 contiguous), strides in bytes, boxes of b0 x b1 x 1, zero fill outside
+int encode_bf16_3d(CUtensorMap *map, const void *base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1,
+                   uint64_t s2, uint32_t b0, uint32_t b1) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+    if (!fn) {
+        hgb::set_cuda_error(cudaErrorNotSupported);
+        return HGB_ERR_CUDA;
+    }
+    cuuint64_t dims[3] = {d0, d1, d2};
+    cuuint64_t strides[2] = {s1, s2};
+    cuuint32_t box[3] = {b0, b1, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        hgb::set_cuda_error(cudaErrorInvalidValue);
+        return HGB_ERR_INVALID_ARGUMENT;
+    }
+    return HGB_OK;
+}
+
+int launch_fwd_tma(const FwdOp &op, long x_member_stride_elems, int members, int *status, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t err = cudaFuncSetAttribute(k_mlp_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
+        if (err != cudaSuccess) {
+            hgb::set_cuda_error(err);
+            return HGB_ERR_CUDA;
+        }
+        attr_set = true;
+    }
+    CUtensorMap xmap, wmap;
+    const uint64_t xrow = (uint64_t)op.ldx * 2;
+    const int x_member = x_member_stride_elems != 0;
+    int rc = encode_bf16_3d(&xmap, op.x, (uint64_t)op.K, (uint64_t)op.batch, x_member ? (uint64_t)members : 1, xrow,
+                            x_member ? (uint64_t)x_member_stride_elems * 2 : xrow * (uint64_t)op.batch, 8, TM);
+    if (rc) return rc;
+    rc = encode_bf16_3d(&wmap, op.w, (uint64_t)op.K, (uint64_t)op.N, (uint64_t)members, (uint64_t)op.K * 2,
+                        (uint64_t)op.w_es * 2, 8, FWD_NT);
+    if (rc) return rc;
+    dim3 grid((unsigned)hgb::ceil_div(op.batch, TM), (unsigned)hgb::ceil_div(op.N, FWD_NT), (unsigned)members);
+    k_mlp_fwd_tma<<<grid, THREADS, SMEM_DYN, st>>>(xmap, wmap, op, x_member, status);
+    return hgb::check_launch();
 }
 
 // ---- loss, gradient reduction, optimiser ----------------------------------------------------------
@@ -534,7 +674,6 @@ int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride,
     cudaStream_t st = (cudaStream_t)stream;
     const long hid_es = (long)batch * WIDTH;            // member stride of one layer's hidden buffer
     const long hid_ls = (long)v.E * hid_es;             // layer stride
-    const int tiles = (int)hgb::ceil_div(batch, TM);
     for (int l = 0; l < v.L; l++) {
         FwdOp op{};
         const bool first = l == 0, last = l == v.L - 1;
@@ -557,7 +696,7 @@ int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride,
         op.ldy = WIDTH;
         op.out = last ? out : nullptr;
         op.out_es = (long)batch * v.N[l];
-        int rc = launch_gemm(op, tiles, v.E, d_status, st);
+        int rc = launch_fwd_tma(op, op.x_es, v.E, d_status, st);
         if (rc) return rc;
     }
     return HGB_OK;

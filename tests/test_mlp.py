@@ -95,10 +95,12 @@ def _bf16_tensor(a):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dims,batch", [([16, 32], 200), ([256, 160], 129), ([16, 256], 128), ([64, 48, 32], 300)])
+@pytest.mark.parametrize("dims,batch", [([16, 32], 200), ([256, 160], 129), ([16, 256], 128), ([64, 48, 32], 300),
+                                        ([16, 160], 1)])
 def test_forward_exact_on_small_integers(built_lib, dims, batch):
     """Integer weights, biases and inputs: every tensor-core sum is exact, so the output equals the
-    oracle bit for bit (checks the shared-memory layout, descriptors and TMEM read-back)."""
+    oracle bit for bit (checks the TMA boxes, shared-memory layout, descriptors and TMEM read-back,
+    including rows and columns the boxes fill with zeros)."""
     import torch
     rng = np.random.default_rng(len(dims) * 1000 + batch)
     E = 2
