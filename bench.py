@@ -280,29 +280,22 @@ def run_batched(args, rank=0, world=1):
     """The batched-library workload through the public library API (host parameters in, host arrays
     out): samples rank, rank + world, ... of the library on this rank's GPU.  Returns the object the
     bench line carries (on rank 0; the wall time is the max over ranks)."""
-    import torch
     from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
     n = args.batched_samples
     space = PS_Classic_Phenom_Uniform(nsamples=n, seed=0)
     shapes, nreals = batch.random_shapes(n, seed=0)
     stats = {}
     out = batch.run_library(space, shapes, nreals, nfreqs=NFREQ, nloudest=NLOUD, seed=1,
-                            indices=list(range(rank, n, world)), stats=stats)
-    wall, reals, draws = stats["seconds"], stats["realizations"], stats["draws"]
-    if world > 1:
-        import torch.distributed as dist
-        mx = torch.tensor([wall], dtype=torch.float64, device="cuda")
-        tt = torch.tensor([reals, draws], dtype=torch.float64, device="cuda")
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt, op=dist.ReduceOp.SUM)
-        wall, reals, draws = float(mx.item()), float(tt[0].item()), float(tt[1].item())
+                            indices=batch.shard_indices(n, rank, world), stats=stats)
+    job = batch.reduce_stats(stats)                       # max wall time, summed work over the replicas
+    wall, reals, draws = job["seconds"], job["realizations"], job["draws"]
     d2h = sum(sum(v.nbytes for k, v in r.items() if isinstance(v, np.ndarray)) for r in out if r is not None)
     tuning = stats.get("tuning") or {}
     table = tuning.get("table", {})
     ones = [v for k, v in table.items() if k.split(",")[0] == "1"]
     one = max(ones) if ones else None
     best = table.get(f"{stats['workers']},{stats['waves']}")
-    return {"workload": BATCH_CONFIG, "samples": n, "failed": stats["failed"], "seconds": wall,
+    return {"workload": BATCH_CONFIG, "samples": n, "failed": job["failed"], "seconds": wall,
             "value": reals / wall, "unit": UNIT, "samples_per_s": n / wall, "draws_per_s": draws / wall,
             "realizations": int(reals), "schedule": {"workers": stats["workers"], "waves": stats["waves"]},
             "autotune_draws_per_s": table,

@@ -83,6 +83,37 @@ def make_jobs(space, shapes=None, nreals=None, seed=0, indices=None):
     return jobs
 
 
+def shard_indices(nsamples, rank, world):
+    """The samples replica ``rank`` of ``world`` runs: round robin, so every sample runs exactly once
+    and the replicas' mixes of grid shapes are alike.  Sample keys depend on the index only, so the
+    union of the shards equals a one-GPU run."""
+    if not (0 <= rank < world):
+        raise ValueError(f"rank {rank} outside world of {world}")
+    return list(range(rank, int(nsamples), world))
+
+
+def reduce_stats(stats, device=None):
+    """Whole-job view of the ``stats`` of one replica's :func:`run_library` under torch.distributed:
+    the longest wall time, and the summed samples, failures, realizations and draws.  Without an
+    initialised process group (or with one rank) the stats are returned unchanged."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return dict(stats)
+    if device is None:
+        device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    longest = torch.tensor([float(stats["seconds"])], dtype=torch.float64, device=device)
+    sums = torch.tensor([stats["samples"], stats["failed"], stats["realizations"], stats["draws"]],
+                        dtype=torch.float64, device=device)
+    dist.all_reduce(longest, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sums, op=dist.ReduceOp.SUM)
+    out = dict(stats)
+    sums = sums.cpu().tolist()
+    out.update(seconds=float(longest.item()), samples=int(sums[0]), failed=int(sums[1]), realizations=int(sums[2]),
+               draws=float(sums[3]), ranks=dist.get_world_size())
+    return out
+
+
 def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=None):
     """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: result or None}
     and {index: exception} for samples that failed.  A result is run_model's dict, or ``reduce`` of it."""
