@@ -10,8 +10,9 @@ Poisson realizations with the loudest split).  value = realizations / s.
 
 The line also carries ``batched``: a whole library of 512 Latin-hypercube samples of
 PS_Classic_Phenom_Uniform, each on its own grid (40-91 per axis) with its own realization count
-(100-1000), run through the batched library API (realizations/s over the library), and
-``emulator``: the MLP ensemble trained on a GPU-SAM library of the same space at the default grid,
+(100-1000), run through the batched library API (realizations/s over the library); ``warm``: the
+same workload on a reused model instance (density, scatter and hardening norm cached); ``highres``:
+the 181x161x201, 100-frequency, 10^4-realization workload; and ``emulator``: the MLP ensemble trained on a GPU-SAM library of the same space at the default grid,
 its held-out accuracy and query time against the plain GPU SAM's time for the same query.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -59,11 +60,14 @@ def dist_env():
 # GPU arm
 # ------------------------------------------------------------------------------------------------
 
-def make_model(H, C):
+def make_model(H, C, shape=SHAPE, edges=None):
+    """The bench model (SAM + hardening); ``edges`` replaces the grid's (mtot, mrat, redz) edges."""
     gsmf = H.sams.GSMF_Schechter(phi0=-2.77, mchar0_log10=11.24, alpha0=-1.24)
     mmb = H.host_relations.MMBulge_KH2013(mamp_log10=8.69, mplaw=1.17, scatter_dex=0.28)
     sam = H.sams.Semi_Analytic_Model(gsmf=gsmf, gpf=H.sams.GPF_Power_Law(), gmt=H.sams.GMT_Power_Law(),
-                                     mmbulge=mmb, shape=SHAPE)
+                                     mmbulge=mmb, shape=shape)
+    if edges is not None:
+        sam.mtot, sam.mrat, sam.redz = (np.asarray(e, dtype=np.float64) for e in edges)
     hard = H.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * C.GYR, sepa_init=1.0e3 * C.PC, rchar=100.0 * C.PC,
                                           gamma_inner=-1.0, gamma_outer=2.5)
     return sam, hard
@@ -178,6 +182,23 @@ def run_gpu(args):
         ms = float(tt.item())
     value = world * NREALS / (ms / 1e3)
 
+    # ---- warm: the same model instance again (density, scatter and hardening norm cached on it, as
+    # the reference caches static_binary_density); dbn, integration, strain, sort and realizations
+    # recomputed every step
+    warm_sam, warm_hard = make_model(H, C)
+    warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0, return_torch=True)
+    barrier()
+    w0 = torch.cuda.Event(enable_timing=True)
+    w1 = torch.cuda.Event(enable_timing=True)
+    w0.record()
+    for i in range(args.steps):
+        flush.zero_()
+        warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0 + 7919 + i, return_torch=True)
+    w1.record()
+    barrier()
+    warm_ms = w0.elapsed_time(w1) / args.steps
+    del warm_sam, warm_hard
+
     # ---- e2e: the public numpy API (results copied to host every step)
     barrier()
     te0 = time.perf_counter()
@@ -238,8 +259,17 @@ def run_gpu(args):
         pass
 
     batched = run_batched(args, rank, world) if args.batched_samples > 0 else None
+    highres = None
+    if args.highres_steps > 0 and rank == 0:
+        hargs = argparse.Namespace(**vars(args))
+        hargs.steps = args.highres_steps
+        highres = run_highres(hargs)
+        torch.cuda.empty_cache()
     emulator = run_emulator(args) if (args.emulator_samples > 0 and rank == 0) else None
-    cpu = cpu_baseline_sample(args) if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
+    cpu = hc_error = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu, keep = cpu_baseline_sample(args)
+        hc_error = hc_error_vs_oracle(keep)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -262,7 +292,12 @@ def run_gpu(args):
                                   "from ncu, see profiles/)")},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "hc_error": hc_error,
+            "warm": {"value": world * NREALS / (warm_ms / 1e3), "unit": UNIT, "ms_per_step": warm_ms,
+                     "note": "same model instance each step: density, M-Mbulge scatter and hardening "
+                             "normalisation cached on it; everything from the dbn stage on recomputed"},
             "batched": batched,
+            "highres": highres,
             "emulator": emulator,
         }
         print(json.dumps(line))
@@ -385,8 +420,9 @@ SAMPLE_Z = 11
 SAMPLE_R = 3
 
 
-def _oracle_sample(seed, nreals):
-    """Times the oracle path on the sample grid (91 x 81 x 11): stage seconds."""
+def _oracle_sample(seed, nreals, keep=None):
+    """Times the oracle path on the sample grid (91 x 81 x 11): stage seconds.  With ``keep`` (a
+    dict) it also receives the sample's edges, frequency edges, grids and loudest-first order."""
     from oracle import sam_oracle as O
     from holodeck_gb300 import constants as C
     shape = (SHAPE[0], SHAPE[1], SAMPLE_Z)
@@ -416,6 +452,9 @@ def _oracle_sample(seed, nreals):
     t0 = time.perf_counter()
     O.loudest_hc_from_sorted(number, h2fdf, nreals, NLOUD, order, seed=seed)
     t["realize"] = time.perf_counter() - t0
+    if keep is not None:
+        keep.update(edges=[mtot, mrat, redz], fobs_gw_edges=fe, number=number, h2fdf=h2fdf, order=order,
+                    redz_final=rf)
     return t
 
 
@@ -429,12 +468,43 @@ def _extrapolate(t, nreals_sampled):
 
 
 def cpu_baseline_sample(args):
-    t = _oracle_sample(seed=7, nreals=SAMPLE_R)
+    keep = {}
+    t = _oracle_sample(seed=7, nreals=SAMPLE_R, keep=keep)
     total, grid, per_real = _extrapolate(t, SAMPLE_R)
     return {"value": NREALS / total, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": (f"oracle on grid 91x81x{SAMPLE_Z} with {SAMPLE_R} realizations, extrapolated linearly in "
                        f"redshift bins and realizations: grid stages {grid:.1f} s + {per_real:.2f} s/realization "
-                       f"({', '.join(f'{k} {v:.2f}s' for k, v in t.items())})")}
+                       f"({', '.join(f'{k} {v:.2f}s' for k, v in t.items())})")}, keep
+
+
+def hc_error_vs_oracle(keep, nreals=8):
+    """The GPU path's strain against the FP64 oracle on the CPU baseline's sample model (the bench
+    model on a 91 x 81 x 11 grid, 40 frequencies): the oracle's grids and numpy-PCG64 Poisson counts
+    replayed through the public gwb(); max relative error of hc_ss and hc_bg, and of the number and
+    strain grids."""
+    import holodeck_gb300 as H
+    from holodeck_gb300 import constants as C
+    from oracle import sam_oracle as O
+    sam, hard = make_model(H, C, shape=tuple(len(e) for e in keep["edges"]), edges=keep["edges"])
+    fe = keep["fobs_gw_edges"]
+    counts = O.replay_counts(keep["number"], keep["order"], nreals, 11)
+    ss_o, bg_o = O.ss_gws_redz(keep["edges"] + [fe / 2.0], keep["redz_final"], keep["number"], nreals, NLOUD,
+                               counts=counts)
+    ss, bg = sam.gwb(fe, hard=hard, realize=nreals, loudest=NLOUD, replay=counts, order=keep["order"])
+    rf, dn = sam._dbn_device(hard, O.midpoints(fe) / 2.0)
+    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf)
+
+    def rel(a, b):
+        a, b = np.asarray(a), np.asarray(b)
+        scale = np.maximum(np.abs(a), np.abs(b))
+        m = scale > 0
+        return float((np.abs(a - b)[m] / scale[m]).max()) if m.any() else 0.0
+
+    return {"case": (f"bench model on the 91x81x{SAMPLE_Z} grid, {NFREQ} frequencies, {nreals} realizations replayed "
+                     "from numpy PCG64 Poisson draws, against the FP64 CPU oracle"),
+            "hc_ss_max_rel": rel(ss, ss_o), "hc_bg_max_rel": rel(bg, bg_o),
+            "number_max_rel": rel(number.cpu().numpy(), keep["number"]),
+            "h2fdf_max_rel": rel(h2fdf.cpu().numpy(), keep["h2fdf"])}
 
 
 def _worker(args):
@@ -626,6 +696,8 @@ def main():
     ap.add_argument("--emulator-steps", type=int, default=6000, help="emulator training steps (batch 512)")
     ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
     ap.add_argument("--mlp-profile", action="store_true", help="untimed emulator-network kernels (for ncu)")
+    ap.add_argument("--highres-steps", type=int, default=1,
+                    help="timed evaluations of the high-resolution measurement carried by the bench line (0: skip)")
     ap.add_argument("--highres", action="store_true",
                     help="only the high-resolution workload (181x161x201, 100 frequencies, 10^4 realizations)")
     ap.add_argument("--emulator-cache", default=None,
