@@ -503,6 +503,7 @@ def hc_error_vs_oracle(keep, nreals=8):
     return {"case": (f"bench model on the 91x81x{SAMPLE_Z} grid, {NFREQ} frequencies, {nreals} realizations replayed "
                      "from numpy PCG64 Poisson draws, against the FP64 CPU oracle"),
             "hc_ss_max_rel": rel(ss, ss_o), "hc_bg_max_rel": rel(bg, bg_o),
+            "hc_bg_max_rel_per_freq": [rel(bg[f], bg_o[f]) for f in range(bg.shape[0])],
             "number_max_rel": rel(number.cpu().numpy(), keep["number"]),
             "h2fdf_max_rel": rel(h2fdf.cpu().numpy(), keep["h2fdf"])}
 

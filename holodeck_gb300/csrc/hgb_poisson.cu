@@ -1525,9 +1525,13 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
 // Waves of resident k_bulk blocks (six per SM) that the chunk count aims for; set by hgb_set_bulk_waves.
+// A block's cost depends strongly on its frequency (the lowest frequencies hold most of the
+// occupied bins), so many short blocks balance the SMs better than a few long ones: on the
+// 91x81x101 grid with 40 frequencies and 1000 realizations the kernel takes 33.9 / 31.3 / 29.9 /
+// 29.7 / 29.2 / 29.2 ms at 2 / 4 / 6 / 8 / 12 / 16 waves on a GB300.
 // Workspace sizes are always computed for HGB_BULK_WAVES_MAX, so a change between a workspace query
 // and a launch only leaves part of the workspace unused.
-std::atomic<int> g_bulk_waves{2};
+std::atomic<int> g_bulk_waves{12};
 
 int bulk_waves() { return g_bulk_waves.load(std::memory_order_relaxed); }
 

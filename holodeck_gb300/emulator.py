@@ -108,8 +108,8 @@ class MLPEnsemble:
         self.struct.params = self.params.data_ptr()
         self.struct.weights = self.weights.data_ptr()
 
-    def _buffers_for(self, batch, train):
-        key = (int(batch), bool(train))
+    def _buffers_for(self, batch, train, owner=None):
+        key = (int(batch), bool(train), owner)
         buf = self._buffers.get(key)
         if buf is None:
             t = D.torch()
@@ -125,12 +125,14 @@ class MLPEnsemble:
             self._buffers[key] = buf
         return buf
 
-    def forward(self, x, train=False, member_stride=0):
-        """Outputs [E, B, n_out] (fp32) for bf16 inputs x [B, dims[0]] (one batch for all members)."""
+    def forward(self, x, train=False, member_stride=0, owner=None):
+        """Outputs [E, B, n_out] (fp32) for bf16 inputs x [B, dims[0]] (one batch for all members).
+        The activation buffers are per (batch, train, owner): a captured graph passes its own owner
+        so that eager calls never write into the buffers its replays read."""
         t = D.torch()
         assert x.dtype == t.bfloat16 and x.is_contiguous() and x.shape[-1] == self.dims[0]
         batch = int(x.shape[-2])
-        buf = self._buffers_for(batch, train)
+        buf = self._buffers_for(batch, train, owner)
         N.call("hgb_mlp_forward", ctypes.byref(self.struct), N.ptr(x), int(member_stride), batch, N.ptr(buf["act"]),
                N.ptr(buf["pre"]), N.ptr(buf["out"]), self.status.ptr, N.stream_handle())
         N.add_launches(self.L)
@@ -140,7 +142,7 @@ class MLPEnsemble:
         """Forward + backward of one batch: loss [E] (device) and self.grad [E, P]."""
         batch = int(x.shape[-2])
         out = self.forward(x, train=True)
-        buf = self._buffers[(batch, True)]
+        buf = self._buffers[(batch, True, None)]
         N.call("hgb_mlp_backward", ctypes.byref(self.struct), N.ptr(x), 0, batch, N.ptr(buf["act"]),
                N.ptr(buf["pre"]), N.ptr(out), N.ptr(target), 0, N.ptr(self.grad), N.ptr(buf["loss"]),
                N.ptr(buf["ws"]), buf["ws_bytes"], self.status.ptr, N.stream_handle())
@@ -298,12 +300,12 @@ class _GraphedForward:
         self.h_out_np = self.h_out.numpy()
         self.stream = t.cuda.Stream(device=dev)
         with t.cuda.stream(self.stream):
-            emu.net.forward(self.d_in)      # eager pass: lazy kernel attributes, buffers
+            emu.net.forward(self.d_in, owner=self)   # eager pass: lazy kernel attributes, this graph's buffers
             self.stream.synchronize()
             self.graph = t.cuda.CUDAGraph()
             with t.cuda.graph(self.graph, stream=self.stream):
                 self.d_in.copy_(self.h_in, non_blocking=True)
-                out = emu.net.forward(self.d_in)
+                out = emu.net.forward(self.d_in, owner=self)
                 self.h_out.copy_(out, non_blocking=True)
         self.stream.synchronize()
 

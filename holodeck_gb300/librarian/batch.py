@@ -38,7 +38,7 @@ _TUNING_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__fi
 _TUNING_LOCK = threading.Lock()
 
 #: (workers, waves) schedules the autotuner tries
-CANDIDATES = ((1, 2), (2, 2), (4, 2), (6, 2), (8, 2), (4, 1), (6, 1), (4, 3), (6, 3))
+CANDIDATES = ((1, 12), (2, 12), (4, 12), (6, 12), (8, 12), (4, 4), (6, 4), (6, 8), (6, 16))
 
 
 def sample_seed(seed, index):
@@ -234,7 +234,7 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
 
     ``shapes`` / ``nreals``: per-sample lists or one value each (see :func:`make_jobs`).  ``seed``
     keys every sample's realizations (:func:`sample_seed`).  ``workers`` / ``waves`` fix the
-    schedule; otherwise it comes from :func:`autotune` (``tune=True``) or defaults to (3, 2).
+    schedule; otherwise it comes from :func:`autotune` (``tune=True``) or defaults to (6, 12).
     ``stats``, when a dict, receives the schedule, wall time, sample count, realizations and draws.
     ``reduce``, when given, maps each sample's dict to what is kept (on the worker, as soon as the
     sample is done), so large libraries need not hold every realization in host memory.
@@ -250,8 +250,8 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
             workers = tuned["workers"] if workers is None else workers
             waves = tuned["waves"] if waves is None else waves
         else:
-            workers = 3 if workers is None else workers
-            waves = 2 if waves is None else waves
+            workers = 6 if workers is None else workers
+            waves = 12 if waves is None else waves
     lib = N.load()
     old_waves = lib.hgb_get_bulk_waves()
     N.check(lib.hgb_set_bulk_waves(int(waves)), "hgb_set_bulk_waves")

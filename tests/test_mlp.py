@@ -164,7 +164,7 @@ def test_backward_matches_oracle(built_lib):
     t = rng.normal(size=(batch, 32)).astype(np.float32)
     loss = net.gradients(_bf16_tensor(x), torch.as_tensor(t, device="cuda")).cpu().numpy()
     grad = net.grad.cpu().numpy()
-    out = net._buffers[(batch, True)]["out"].cpu().numpy()
+    out = net._buffers[(batch, True, None)]["out"].cpu().numpy()
     net.check_status()
     for m in range(E):
         exp_loss, grads = MO.backward(layers[m], x, t)
