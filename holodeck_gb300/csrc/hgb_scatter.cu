@@ -81,20 +81,29 @@ __global__ void k_gradients(hgb_scatter_plan P, const double *__restrict__ dens,
 // The same solve with the slice's values and gradients in shared memory, indexed by level-order
 // position (a level's points are contiguous), for grids whose state fits on one SM.  GB300's FP64
 // units belong to the four SM sub-partitions and charge each warp instruction in full however few
-// lanes are active, so the block has four warps, one per sub-partition: a level's points (about 20
-// at 91x81) share the lanes of every warp, warp w sums the terms of edges w, w+4, w+8, ... of its
-// point, and warp 0 adds the four partial sums and updates the point.  The static data of the next
-// level (each warp's first LV_REG edges of its point, warp 0's inverse normal matrix) is loaded into
-// registers while the current level computes.  Per point the terms are those of k_gradients; only
-// the grouping of the neighbour sum differs (four interleaved partial sums).
+// lanes are active, so the block has four warps, one per sub-partition, and the per-level work is
+// spread so that no sub-partition carries much more than a quarter of it:
+//   * a level's points (about 20 at 91x81) share the lanes of every warp; warp w sums the terms of
+//     edges o, o+4, o+8, ... of its point with o = (w + 2) mod 4, so an interior point's six edges
+//     put two terms on warps 2 and 3 and one on warps 0 and 1;
+//   * warps 0 and 1 add the four partial sums and solve the x and the y component of the point's
+//     2x2 system respectively;
+//   * warp 2 evaluates the convergence test of the previous 32 points (their changes and magnitudes,
+//     double-buffered in shared memory) while warps 0 and 1 update the current ones.
+// The static data of the next level (each warp's first LV_REG edges of its point, the rows of the
+// inverse normal matrix that warps 0 and 1 use) is loaded into registers while the current level
+// computes.  Per point the terms and the test are those of k_gradients; only the grouping of the
+// neighbour sum differs (four interleaved partial sums).
 constexpr int LV_WARPS = 4;
-constexpr int LV_REG = 3;   // edges w, w+4, w+8 per warp: interior points have 6 neighbours
+constexpr int LV_REG = 3;   // edges o, o+4, o+8 per warp: interior points have 6 neighbours
+
+__device__ __forceinline__ int lv_edge_offset(int warp) { return (warp + 2) & (LV_WARPS - 1); }
 
 struct LvPre {
     int e0, e1;
     int idx[LV_REG];
     double2 w01[LV_REG], w23[LV_REG];
-    double2 q01, q23;
+    double2 q;   // warps 0 / 1: row 0 / 1 of the point's inverse normal matrix
 };
 
 __device__ __forceinline__ void lv_load(const hgb_scatter_plan &P, const int *eptr, int p, bool active, int warp,
@@ -103,17 +112,14 @@ __device__ __forceinline__ void lv_load(const hgb_scatter_plan &P, const int *ep
     x.e1 = active ? eptr[p + 1] : 0;
 #pragma unroll
     for (int k = 0; k < LV_REG; k++) {
-        const int e = x.e0 + warp + LV_WARPS * k;
+        const int e = x.e0 + lv_edge_offset(warp) + LV_WARPS * k;
         if (e < x.e1) {
             x.idx[k] = __ldg(P.lv_nbr + e);
             x.w01[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
             x.w23[k] = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
         }
     }
-    if (active && warp == 0) {
-        x.q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
-        x.q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
-    }
+    if (active && warp < 2) x.q = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2 * warp));   // row `warp`
 }
 
 __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_plan P, const double *__restrict__ dens,
@@ -121,6 +127,7 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                                                                   double *__restrict__ grads, int *d_status) {
     extern __shared__ double sm[];
     __shared__ double psx[LV_WARPS][32], psy[LV_WARPS][32];
+    __shared__ double chg[2][2][32], mag[2][2][32];   // [chunk parity][component][lane]: |change|, |new value|
     __shared__ int s_over;
     const int z = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int n = P.n_mtot * P.n_mrat;
@@ -145,8 +152,18 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
     bool converged = false;
     LvPre nxt;
     lv_load(P, eptr, lptr[0] + lane, lane < lptr[1] - lptr[0], warp, nxt);
+    // exact test of one chunk's points from the buffered changes and magnitudes (warp 2)
+    auto test_chunk = [&](int b, bool over) {
+        const double change = fmax(chg[b][0][lane], chg[b][1][lane]);
+        const double scale = fmax(1.0, fmax(mag[b][0][lane], mag[b][1][lane]));
+        // relative change, divided out only where the comparison with the tolerance is close (the
+        // decision is that of change / scale < tol)
+        if (change >= tol_lo * scale) over = over || (change / scale >= P.grad_tol);
+        return over;
+    };
     for (int it = 0; it < P.grad_maxiter; it++) {
-        bool over = false;   // (warp 0) some point changed by >= grad_tol (relative) in this sweep
+        bool over = false;   // (warp 2) some point changed by >= grad_tol (relative) in this sweep
+        int kc = 0;          // chunks updated so far in this sweep
         for (int lev = 0; lev < nlev; lev++) {
             const int p0 = lptr[lev], p1 = lptr[lev + 1];
             const LvPre cur = nxt;
@@ -163,7 +180,7 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                 if (act) {
                     const double fi = f[p];
                     const int e0 = pre ? cur.e0 : eptr[p], e1 = pre ? cur.e1 : eptr[p + 1];
-                    int e = e0 + warp;
+                    int e = e0 + lv_edge_offset(warp);
                     if (pre) {
 #pragma unroll
                         for (int k = 0; k < LV_REG; k++) {
@@ -189,31 +206,29 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                 psx[warp][lane] = sx;
                 psy[warp][lane] = sy;
                 __syncthreads();
-                if (warp == 0 && act) {
-                    const double tx = ((psx[0][lane] + psx[1][lane]) + psx[2][lane]) + psx[3][lane];
-                    const double ty = ((psy[0][lane] + psy[1][lane]) + psy[2][lane]) + psy[3][lane];
-                    double2 q01, q23;
-                    if (pre) {
-                        q01 = cur.q01;
-                        q23 = cur.q23;
-                    } else {
-                        q01 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p));
-                        q23 = __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2));
+                const int b = kc & 1;
+                if (warp < 2) {   // warp 0 solves the x component, warp 1 the y component
+                    double dv = 0.0, av = 0.0;
+                    if (act) {
+                        const double tx = ((psx[0][lane] + psx[1][lane]) + psx[2][lane]) + psx[3][lane];
+                        const double ty = ((psy[0][lane] + psy[1][lane]) + psy[2][lane]) + psy[3][lane];
+                        const double2 q = pre ? cur.q : __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2 * warp));
+                        const double nv = q.x * tx + q.y * ty;
+                        dv = fabs(nv - g[2 * p + warp]);
+                        av = fabs(nv);
+                        g[2 * p + warp] = nv;
                     }
-                    const double nx = q01.x * tx + q01.y * ty;
-                    const double ny = q23.x * tx + q23.y * ty;
-                    // relative change, divided out only where the comparison with the tolerance is
-                    // close (the decision is that of change / scale < tol)
-                    const double change = fmax(fabs(nx - g[2 * p]), fabs(ny - g[2 * p + 1]));
-                    const double scale = fmax(1.0, fmax(fabs(nx), fabs(ny)));
-                    g[2 * p] = nx;
-                    g[2 * p + 1] = ny;
-                    if (change >= tol_lo * scale) over = over || (change / scale >= P.grad_tol);
+                    chg[b][warp][lane] = dv;
+                    mag[b][warp][lane] = av;
+                } else if (warp == 2 && kc > 0) {
+                    over = test_chunk(b ^ 1, over);   // the previous chunk, while this one updates
                 }
                 __syncthreads();
+                kc++;
             }
         }
-        if (warp == 0) {
+        if (warp == 2) {
+            if (kc > 0) over = test_chunk((kc - 1) & 1, over);   // the sweep's last chunk
             const bool any = __any_sync(0xffffffffu, over);
             if (lane == 0) s_over = any ? 1 : 0;
         }
@@ -363,7 +378,7 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     int dev = 0, smem_optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 4096 <= (size_t)smem_optin) {
+    if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 8192 <= (size_t)smem_optin) {
         cudaFuncSetAttribute(k_gradients_lv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_smem);
         k_gradients_lv<<<n_redz, 32 * LV_WARPS, lv_smem, st>>>(P, dens, n_redz, vals, grads, d_status);
     } else {
