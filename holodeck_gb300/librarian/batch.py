@@ -38,7 +38,7 @@ _TUNING_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__fi
 _TUNING_LOCK = threading.Lock()
 
 #: (workers, waves) schedules the autotuner tries
-CANDIDATES = ((1, 12), (2, 12), (4, 12), (6, 12), (8, 12), (4, 4), (6, 4), (6, 8), (6, 16))
+CANDIDATES = ((1, 12), (2, 12), (4, 12), (6, 12), (8, 12), (10, 12), (12, 12), (8, 8), (8, 16))
 
 
 def sample_seed(seed, index):
