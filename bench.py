@@ -381,6 +381,8 @@ def run_emulator(args):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     mean, spread, inside = emu.predict(sp_te.param_samples)
+    spread_p50 = emu.predict(sp_te.param_samples, spread_stats=("log10_hc_p50",))[1]
+    spread_hc = emu.predict(sp_te.param_samples, spread_stats=("log10_hc_p05", "log10_hc_p50", "log10_hc_p95"))[1]
     good = np.all(np.isfinite(y_te), axis=(1, 2)) & np.all(np.isfinite(y_te2), axis=(1, 2))
     err = np.abs(mean - y_te)[good]
     u_tr, u_te = emu.unit(sp_tr.param_samples[ok]), emu.unit(sp_te.param_samples)
@@ -407,8 +409,15 @@ def run_emulator(args):
             "nearest_sample_median_abs_dlog10": med(err_nn), "realization_noise_median_dlog10": med(noise),
             "ensemble_spread_median_dex": float(np.median(spread)),
             "flagged_fraction_at_0.05dex": float(np.mean(spread > 0.05)),
+            "flagged_fraction_at_0.05dex_by_criterion": {
+                "all_outputs": float(np.mean(spread > 0.05)),
+                "hc_percentiles": float(np.mean(spread_hc > 0.05)),
+                "median_hc": float(np.mean(spread_p50 > 0.05))},
             "query_s_batch1": t_q1, "query_s_per_sample_batch1024": t_qb / 1024,
             "plain_gpu_sam_s": t_plain, "speedup_vs_plain_batch1": t_plain / t_q1,
+            "speedup_vs_plain_batch1_with_fallbacks": {
+                nm: t_plain / (t_q1 + float(np.mean(sv > 0.05)) * t_plain)
+                for nm, sv in (("all_outputs", spread), ("hc_percentiles", spread_hc), ("median_hc", spread_p50))},
             "speedup_vs_plain_batch1024": t_plain / (t_qb / 1024)}
 
 

@@ -248,19 +248,22 @@ class Emulator:
         out = out * self.sd + self.mu
         return out.reshape(out.shape[0], out.shape[1], self.nfreqs, 4)
 
-    def predict(self, params):
+    def predict(self, params, spread_stats=None):
         """(mean (Q, F, 4), spread (Q,), inside (Q,)): the ensemble mean, the largest standard
-        deviation over members of any output (dex), and whether the query lies in the training box."""
+        deviation over members (dex) of the statistics named in ``spread_stats`` (default: all of
+        :data:`STATS`) at any frequency, and whether the query lies in the training box."""
         mem = self.predict_members(params)
         u = self.unit(params)
         inside = np.all((u >= 0.0) & (u <= 1.0), axis=1)
-        return mem.mean(axis=0), mem.std(axis=0).max(axis=(1, 2)), inside
+        cols = list(range(4)) if spread_stats is None else [STATS.index(nm) for nm in spread_stats]
+        return mem.mean(axis=0), mem.std(axis=0)[..., cols].max(axis=(1, 2)), inside
 
-    def query(self, params, fallback=None, max_spread=0.05):
+    def query(self, params, fallback=None, max_spread=0.05, spread_stats=None):
         """Statistics (Q, F, 4) with the plain SAM as fallback: queries outside the training box or
-        with ensemble spread above ``max_spread`` dex are re-solved by ``fallback(param_row) -> (F, 4)``
-        (e.g. :func:`sam_fallback`).  Returns (stats, solved_by_sam mask)."""
-        mean, spread, inside = self.predict(params)
+        with ensemble spread (of ``spread_stats``, see :meth:`predict`) above ``max_spread`` dex are
+        re-solved by ``fallback(param_row) -> (F, 4)`` (e.g. :func:`sam_fallback`).  Returns (stats,
+        solved_by_sam mask)."""
+        mean, spread, inside = self.predict(params, spread_stats=spread_stats)
         redo = (~inside) | (spread > max_spread)
         if fallback is not None:
             for qq in np.flatnonzero(redo):
