@@ -458,16 +458,46 @@ __device__ __forceinline__ void add_bg(SlotsKahan &st, int sl, int t, float x) {
 }
 
 // ---- 1. gather into loudest-first (F, B) order
-__global__ void k_gather_sorted(const double *__restrict__ number, const double *__restrict__ h2fdf,
-                                const int32_t *__restrict__ order, long nb, int nf, double *__restrict__ lam_s,
-                                double *__restrict__ h_s) {
-    long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nb * nf) return;
-    int f = (int)(idx % nf);
-    long k = idx / nf;
-    long src = (long)order[k] * nf + f;
-    lam_s[(long)f * nb + k] = number[src];
-    h_s[(long)f * nb + k] = h2fdf[src];
+// A 32 x 32 tile of (sorted bin, frequency) per block, transposed through shared memory: the reads
+// take 32 consecutive frequencies of one bin's row, the writes 32 consecutive sorted bins of one
+// frequency's row, so both sides are contiguous 256-byte runs.
+constexpr int GT = 32;   // tile edge
+constexpr int GR = 8;    // thread rows (GT x GR threads, GT / GR rows each)
+
+__global__ void __launch_bounds__(GT * GR) k_gather_sorted(const double *__restrict__ number,
+                                                           const double *__restrict__ h2fdf,
+                                                           const int32_t *__restrict__ order, long nb, int nf,
+                                                           double *__restrict__ lam_s, double *__restrict__ h_s) {
+    __shared__ double tl[GT][GT + 1], th[GT][GT + 1];
+    const long k0 = (long)blockIdx.x * GT;
+    const int f0 = blockIdx.y * GT;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+    for (int j = ty; j < GT; j += GR) {   // row j of the tile: bin k0 + j, frequencies f0 + tx
+        const long k = k0 + j;
+        const int f = f0 + tx;
+        if (k < nb && f < nf) {
+            const long src = (long)order[k] * nf + f;
+            tl[j][tx] = number[src];
+            th[j][tx] = h2fdf[src];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = ty; j < GT; j += GR) {   // frequency f0 + j, bins k0 + tx
+        const int f = f0 + j;
+        const long k = k0 + tx;
+        if (k < nb && f < nf) {
+            lam_s[(long)f * nb + k] = tl[tx][j];
+            h_s[(long)f * nb + k] = th[tx][j];
+        }
+    }
+}
+
+void launch_gather_sorted(const double *number, const double *h2fdf, const int32_t *order, long nb, int nf,
+                          double *lam_s, double *h_s, cudaStream_t st) {
+    dim3 grid((unsigned)hgb::ceil_div(nb, GT), (unsigned)hgb::ceil_div(nf, GT));
+    k_gather_sorted<<<grid, dim3(GT, GR), 0, st>>>(number, h2fdf, order, nb, nf, lam_s, h_s);
 }
 
 // ---- 2. cumulative expectation along the sorted bins: C[0] = 0, C[k + 1] = C[k] + max(lambda_k, 0)
@@ -1671,9 +1701,8 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
     char *w = (char *)workspace;
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
-    const long n = n_bins * n_freq;
     const long nfr = (long)n_freq * nreals;
-    k_gather_sorted<<<(unsigned)hgb::ceil_div(n, 256), 256, 0, st>>>(number, h2fdf, order, n_bins, n_freq, lam_s, h_s);
+    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st);
     int rc = hgb::check_launch();
     if (rc) return rc;
     if (mode == HGB_RNG_REPLAY) {
@@ -1747,7 +1776,6 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     char *w = (char *)workspace;
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
-    const long n = n_bins * n_freq;
     const long nfr = (long)n_freq * nreals;
     ParArgs pa{};
     pa.order = order;
@@ -1762,7 +1790,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     pa.nq = n_q;
     pa.nz = n_z;
     pa.sspar = sspar;
-    k_gather_sorted<<<(unsigned)hgb::ceil_div(n, 256), 256, 0, st>>>(number, h2fdf, order, n_bins, n_freq, lam_s, h_s);
+    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st);
     int rc = hgb::check_launch();
     if (rc) return rc;
     if (mode == HGB_RNG_REPLAY) {
