@@ -506,7 +506,7 @@ void launch_gather_sorted(const double *number, const double *h2fdf, const int32
 // k_cum_write scans each segment from the sum of the segments before it.
 constexpr int CUM_THREADS = 1024;
 constexpr int CUM_PER_THREAD = 4;
-constexpr int CUM_SEG = 16;
+constexpr int CUM_SEG = 64;   // segments per frequency: about 8 waves of scan blocks on 152 SMs at 40 frequencies
 
 __device__ __forceinline__ double cum_term(const double *lam, const double *mask, long k) {
     double x = lam[k];
