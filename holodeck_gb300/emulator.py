@@ -34,6 +34,13 @@ HIDDEN_STRIDE = 256
 LOG10_FLOOR = -40.0
 
 
+def bf16_bits(x):
+    """bfloat16 bit patterns (uint16) of values rounded to the nearest bfloat16, ties to even: the
+    conversion the device makes, done on the host for the graphed query path's pinned inputs."""
+    bits = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+    return ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16)
+
+
 def strain_statistics(hc_ss, hc_bg):
     """(F, 4) statistics of one model evaluation from hc_ss (F, R, L) and hc_bg (F, R) (see module)."""
     hc_ss = np.asarray(hc_ss, dtype=np.float64)
@@ -318,10 +325,7 @@ class _GraphedForward:
         q, npar = u.shape
         if q > self.batch:
             raise ValueError(f"at most {self.batch} queries per call")
-        x = (2.0 * u - 1.0).astype(np.float32)
-        bits = x.view(np.uint32)
-        # round to the nearest bfloat16, ties to even (the conversion the eager path makes on the device)
-        self.h_in_bits[:q, :npar] = ((bits + 0x7FFF + ((bits >> 16) & 1)) >> 16).astype(np.uint16).view(np.int16)
+        self.h_in_bits[:q, :npar] = bf16_bits(2.0 * u - 1.0).view(np.int16)
         with t.cuda.stream(self.stream):
             self.graph.replay()
         self.stream.synchronize()
