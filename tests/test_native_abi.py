@@ -48,3 +48,38 @@ def test_product_never_imports_the_oracle():
             if fn.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
                 text = open(os.path.join(dirpath, fn)).read()
                 assert "oracle" not in re.sub(r"#.*|//.*", "", text).replace("the oracle", ""), fn
+
+
+def test_schedule_knob_and_mlp_descriptions_checked_on_the_host(built_lib):
+    """The realization kernels' waves knob and the MLP entry points validate their arguments before
+    any CUDA call."""
+    from holodeck_gb300 import _native as N
+    lib = N.load()
+    before = lib.hgb_get_bulk_waves()
+    assert 1 <= before <= 16
+    for bad in (0, -1, 17):
+        assert lib.hgb_set_bulk_waves(bad) == N.HGB_ERR_INVALID_ARGUMENT
+    assert lib.hgb_get_bulk_waves() == before
+    assert lib.hgb_set_bulk_waves(before) == N.HGB_OK
+
+    net = N.HgbMlp()
+    net.n_layers, net.n_members = 5, 4
+    for ii, d in enumerate([16, 256, 256, 256, 256, 160]):
+        net.dims[ii] = d
+    ref = ctypes.byref(net)
+    # widths 16 -> 4 x 256 -> 160: W then b per layer
+    assert lib.hgb_mlp_param_count(ref) == 16 * 256 + 256 + 3 * (256 * 256 + 256) + 256 * 160 + 160
+    assert lib.hgb_mlp_weight_count(ref) == 16 * 256 + 3 * 256 * 256 + 256 * 160
+    assert lib.hgb_mlp_backward_workspace_bytes(ref, 512) > 0
+    # no parameter buffers: rejected before any launch
+    assert lib.hgb_mlp_forward(ref, ctypes.c_void_p(16), 0, 8, ctypes.c_void_p(16), None, ctypes.c_void_p(16), None,
+                               None) == N.HGB_ERR_INVALID_ARGUMENT
+    for bad_dims in ([6, 256, 160], [16, 272, 160], [16, 8, 160]):   # widths must be multiples of 16 in [16, 256]
+        bad = N.HgbMlp()
+        bad.n_layers, bad.n_members = 2, 1
+        for ii, d in enumerate(bad_dims):
+            bad.dims[ii] = d
+        assert lib.hgb_mlp_param_count(ctypes.byref(bad)) == -1
+    none = N.HgbMlp()
+    none.n_layers, none.n_members = 0, 1
+    assert lib.hgb_mlp_param_count(ctypes.byref(none)) == -1
