@@ -31,6 +31,26 @@ def test_param_space_samples_match_reference():
     assert p["gsmf_mchar0_log10"] == 11.5   # default = the distribution at 0.5
 
 
+def test_param_space_models_on_the_host():
+    """A sample's SAM (built without a device) carries the sample's parameters and the reference's
+    grid edges; the hardening settings the space passes on are the reference's defaults and units."""
+    from holodeck_gb300 import constants as C
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform
+    g = load_golden("ref_param_space.npz")
+    space = PS_Classic_Phenom_Uniform(nsamples=8, sam_shape=(10, 11, 12), seed=0)
+    for ii in (0, 5):
+        pars = {**space.DEFAULTS, **space.param_dict(ii)}
+        sam = space._init_sam(space.sam_shape, pars)
+        for name in ("mtot", "mrat", "redz"):
+            assert rel_err(getattr(sam, name), g[f"s{ii}_{name}"]) < 1e-14, name
+        assert sam._gsmf._phi0 == pars["gsmf_phi0_log10"] and sam._gsmf._alpha0 == pars["gsmf_alpha0"]
+        assert rel_err(sam._gsmf._mchar0, C.MSOL * 10.0 ** pars["gsmf_mchar0_log10"]) < 1e-15
+        assert rel_err(sam._mmbulge._mamp, C.MSOL * 10.0 ** pars["mmb_mamp_log10"]) < 1e-15
+        assert sam._mmbulge._scatter_dex == pars["mmb_scatter_dex"] and sam._mmbulge._mplaw == 1.10
+        assert sam._gmt._time_norm == 0.5 * C.GYR and sam._gpf._frac_norm > 0.0
+    assert space.DEFAULTS["hard_sepa_init"] == 1e4 and space.DEFAULTS["hard_rchar"] == 100.0
+
+
 def test_jobs_seeds_and_shapes():
     from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
     shapes, nreals = batch.random_shapes(512, seed=0)
