@@ -34,6 +34,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "hgb_common.cuh"
@@ -491,14 +492,14 @@ int encode_bf16_3d(CUtensorMap *map, const void *base, uint64_t d0, uint64_t d1,
 }
 
 int launch_fwd_tma(const FwdOp &op, long x_member_stride_elems, int members, int *status, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<bool> attr_set{false};
+    if (!attr_set.load(std::memory_order_acquire)) {
         cudaError_t err = cudaFuncSetAttribute(k_mlp_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
         if (err != cudaSuccess) {
             hgb::set_cuda_error(err);
             return HGB_ERR_CUDA;
         }
-        attr_set = true;
+        attr_set.store(true, std::memory_order_release);
     }
     CUtensorMap xmap, wmap;
     const uint64_t xrow = (uint64_t)op.ldx * 2;
@@ -640,14 +641,14 @@ int check_net(const hgb_mlp *net) {
 
 template <class Op>
 int launch_gemm(const Op &op, int row_tiles, int members, int *status, cudaStream_t st, int splits = 1) {
-    static bool attr_set = false;   // idempotent; set before the first launch of each instantiation
-    if (!attr_set) {
+    static std::atomic<bool> attr_set{false};   // idempotent; set before the first launch of each instantiation
+    if (!attr_set.load(std::memory_order_acquire)) {
         cudaError_t err = cudaFuncSetAttribute(k_mlp_gemm<Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_DYN);
         if (err != cudaSuccess) {
             hgb::set_cuda_error(err);
             return HGB_ERR_CUDA;
         }
-        attr_set = true;
+        attr_set.store(true, std::memory_order_release);
     }
     const int ytiles = Op::COL_TILED ? (int)hgb::ceil_div(op.ncols(), Op::NT) : splits;
     dim3 grid((unsigned)row_tiles, (unsigned)ytiles, (unsigned)members);
