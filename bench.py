@@ -27,7 +27,6 @@ its held-out accuracy and query time against the plain GPU SAM's time for the sa
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess

@@ -23,7 +23,6 @@ import os
 import shutil
 import subprocess
 import sys
-import types
 
 REF_SRC = os.environ.get("HOLODECK_REF_SRC", "/root/reference")
 BUILD_DIR = os.environ.get("HOLODECK_REF_BUILD", "/tmp/hgb_ref_build")
