@@ -1687,7 +1687,7 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
     HGB_CHECK_ARG(nloud <= 255);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || replay);
-    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals <= HGB_MAX_NREALS);
     if (nreals == 0) return HGB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (n_bins == 0) {
@@ -1767,7 +1767,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_REPLAY ? replay != nullptr : scale_log2 != nullptr);
     const long n_bins = (long)n_m * n_q * n_z;
-    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals <= HGB_MAX_NREALS);
     if (nreals == 0) return HGB_OK;
     const size_t need = hgb_loudest_par_workspace_bytes(n_bins, n_freq, nreals, nloud, mode);
     if (!workspace || workspace_bytes < need) return HGB_ERR_WORKSPACE;
@@ -1850,7 +1850,7 @@ int hgb_sam_poisson_gwb(const double *number, const double *hc2, long n_bins, in
     HGB_CHECK_ARG(number && hc2 && gwb && n_bins >= 0 && n_freq >= 1 && nreals >= 0);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || mode == HGB_RNG_REPLAY);
     HGB_CHECK_ARG(mode == HGB_RNG_PHILOX || replay);
-    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals < (1 << 30));
+    HGB_CHECK_ARG(n_bins < (1L << 31) - 1 && n_freq <= 65535 && nreals <= HGB_MAX_NREALS);
     if (nreals == 0) return HGB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (n_bins == 0) {

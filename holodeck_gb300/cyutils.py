@@ -30,6 +30,34 @@ def _check_threshold(normal_threshold):
         raise ValueError(f"normal_threshold={normal_threshold}: only the reference default 1e10 is supported")
 
 
+def checked_order(order, n_bins, dev=None):
+    """A caller-supplied loudest-first order as a device int32 tensor, after checking that it is a
+    permutation of range(n_bins): the realization kernels index the grids with it, so a short array
+    or an out-of-range index must stop here, as numpy's indexing stops the reference."""
+    t = D.torch()
+    n_bins = int(n_bins)
+    if D.is_torch(order):
+        flat = order.reshape(-1).to(t.int64)       # checked where it lives
+        lo_hi = (lambda: (int(flat.min().item()), int(flat.max().item())))
+        once = (lambda: int(t.bincount(flat, minlength=n_bins).max().item()) == 1)
+    else:
+        flat = np.asarray(order).reshape(-1)       # host data: checked before any device work
+        if flat.size and not np.issubdtype(flat.dtype, np.integer):
+            raise ValueError(f"order must hold integer bin indices, got {flat.dtype}")
+        flat = flat.astype(np.int64)
+        lo_hi = (lambda: (int(flat.min()), int(flat.max())))
+        once = (lambda: int(np.bincount(flat, minlength=n_bins).max()) == 1)
+    if int(flat.shape[0]) != n_bins:
+        raise ValueError(f"order holds {flat.shape[0]} indices; the grid has {n_bins} bins")
+    if n_bins:
+        lo, hi = lo_hi()
+        if lo < 0 or hi >= n_bins:
+            raise ValueError(f"order indices must lie in [0, {n_bins}); got [{lo}, {hi}]")
+        if not once():
+            raise ValueError("order must visit every bin exactly once")
+    return D.as_device(flat, dev, dtype=t.int32)
+
+
 def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=None, status=None, freq_offset=0,
                    out=None):
     """Device (hc2ss[F, R, L], hc2bg[F, R]) from device number/h2fdf (B, F) and order (B,) int32.
@@ -52,6 +80,8 @@ def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=Non
             raise ValueError("out must be contiguous (F, R, L) and (F, R) float64 tensors")
     if freq_offset and replay is not None:
         raise ValueError("freq_offset applies to Philox draws only")
+    if order.dtype != t.int32 or int(order.numel()) != nb or order.device != dev:
+        raise ValueError(f"order must be an int32 tensor of {nb} bin indices on {dev} (see checked_order)")
     mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
     rep = None
     if replay is not None:
@@ -78,8 +108,7 @@ def loudest_hc_from_sorted(number, h2fdf, nreals, nloudest, msort, qsort, zsort,
     num = D.as_device(number).reshape(-1, shape[-1])
     hh = D.as_device(h2fdf).reshape(-1, shape[-1])
     ms, qs, zs = [np.asarray(D.to_host(v) if D.is_torch(v) else v, dtype=np.int64) for v in (msort, qsort, zsort)]
-    order = np.ravel_multi_index((ms, qs, zs), shape[:3])
-    order_t = D.as_device(order, dtype=D.torch().int32)
+    order_t = checked_order(np.ravel_multi_index((ms, qs, zs), shape[:3]), num.shape[0], num.device)
     st = D.StatusWord()
     ss, bg = loudest_device(num, hh, int(nreals), int(nloudest), order_t, seed=seed, replay=replay, status=st)
     _raise_status(st)
@@ -139,6 +168,8 @@ def loudest_par_device(number, h2fdf, nreals, nloudest, order, mt, mr, rz, grids
     hc2bg = t.empty((nf, nreals), dtype=t.float64, device=dev)
     sspar = t.empty((4, nf, nreals, nloudest), dtype=t.float64, device=dev)
     bgpar = t.empty((7, nf, nreals), dtype=t.float64, device=dev)
+    if order.dtype != t.int32 or int(order.numel()) != nb or order.device != dev:
+        raise ValueError(f"order must be an int32 tensor of {nb} bin indices on {dev} (see checked_order)")
     mode = N.RNG_PHILOX if replay is None else N.RNG_REPLAY
     rep = None
     if replay is not None:
@@ -178,7 +209,7 @@ def loudest_hc_and_par_from_sorted_redz(number, h2fdf, nreals, nloudest, mt, mr,
     scales = t.tensor([_frexp_exponent(D.to_host(g)[D.to_host(hh) != 0]) for g in grids], dtype=t.int32,
                       device=num.device)
     ms, qs, zs = [np.asarray(D.to_host(v) if D.is_torch(v) else v, dtype=np.int64) for v in (msort, qsort, zsort)]
-    order = D.as_device(np.ravel_multi_index((ms, qs, zs), shape[:3]), dtype=t.int32)
+    order = checked_order(np.ravel_multi_index((ms, qs, zs), shape[:3]), num.numel() // shape[-1], num.device)
     st = D.StatusWord()
     out = loudest_par_device(num, hh, int(nreals), int(nloudest), order, D.to_host(mt) if D.is_torch(mt) else mt,
                              D.to_host(mr) if D.is_torch(mr) else mr, D.to_host(rz) if D.is_torch(rz) else rz,

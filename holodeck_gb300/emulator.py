@@ -164,9 +164,16 @@ class MLPEnsemble:
                float(eps), float(weight_decay), N.stream_handle())
         return loss
 
-    def check_status(self):
-        if self.status.read() & N.STATUS_ITERATION_LIMIT:
-            raise N.NativeError("an MLP kernel timed out waiting for the tensor core")
+    def check_status(self, code=None):
+        """Raise if a kernel since the last check gave up waiting for the tensor core (its outputs
+        were not written).  The status word is cleared first, so one timeout does not fail later
+        calls.  ``code``: a status value already read (the graphed path copies it to the host)."""
+        if code is None:
+            code = self.status.read()
+            if code:
+                self.status.reset()
+        if code & N.STATUS_ITERATION_LIMIT:
+            raise N.NativeError("an MLP kernel timed out waiting for the tensor core; its outputs are not valid")
 
     def state(self):
         return dict(dims=np.array(self.dims), members=self.members, params=D.to_host(self.params))
@@ -252,6 +259,7 @@ class Emulator:
     def predict_members(self, params):
         """Per-member statistics (E, Q, F, 4) in log10 units."""
         out = D.to_host(self.net.forward(self.inputs(params)))[..., :self.n_out].astype(np.float64)
+        self.net.check_status()
         out = out * self.sd + self.mu
         return out.reshape(out.shape[0], out.shape[1], self.nfreqs, 4)
 
@@ -269,9 +277,17 @@ class Emulator:
         """Statistics (Q, F, 4) with the plain SAM as fallback: queries outside the training box or
         with ensemble spread (of ``spread_stats``, see :meth:`predict`) above ``max_spread`` dex are
         re-solved by ``fallback(param_row) -> (F, 4)`` (e.g. :func:`sam_fallback`).  Returns (stats,
-        solved_by_sam mask)."""
-        mean, spread, inside = self.predict(params, spread_stats=spread_stats)
-        redo = (~inside) | (spread > max_spread)
+        solved_by_sam mask).  If the network's kernels fail (a tensor-core wait gave up), every query
+        is re-solved by ``fallback``; without one the error is raised."""
+        try:
+            mean, spread, inside = self.predict(params, spread_stats=spread_stats)
+            redo = (~inside) | (spread > max_spread)
+        except N.NativeError:
+            if fallback is None:
+                raise
+            nq = np.atleast_2d(params).shape[0]
+            mean = np.full((nq, self.nfreqs, 4), np.nan)
+            redo = np.ones(nq, dtype=bool)
         if fallback is not None:
             for qq in np.flatnonzero(redo):
                 mean[qq] = fallback(np.atleast_2d(params)[qq])
@@ -308,15 +324,21 @@ class _GraphedForward:
         self.d_in = t.zeros((self.batch, INPUT_PAD), dtype=t.bfloat16, device=dev)
         self.h_out = t.zeros((emu.net.members, self.batch, emu.n_pad), dtype=t.float32).pin_memory()
         self.h_out_np = self.h_out.numpy()
+        # the kernels' status word travels back with the outputs; it is cleared at the start of each
+        # replay, so every call reports only its own kernels
+        self.h_status = t.zeros(1, dtype=t.int32).pin_memory()
         self.stream = t.cuda.Stream(device=dev)
         with t.cuda.stream(self.stream):
             emu.net.forward(self.d_in, owner=self)   # eager pass: lazy kernel attributes, this graph's buffers
             self.stream.synchronize()
+            emu.net.check_status()
             self.graph = t.cuda.CUDAGraph()
             with t.cuda.graph(self.graph, stream=self.stream):
+                emu.net.status.t.zero_()
                 self.d_in.copy_(self.h_in, non_blocking=True)
                 out = emu.net.forward(self.d_in, owner=self)
                 self.h_out.copy_(out, non_blocking=True)
+                self.h_status.copy_(emu.net.status.t, non_blocking=True)
         self.stream.synchronize()
 
     def __call__(self, params):
@@ -329,6 +351,7 @@ class _GraphedForward:
         with t.cuda.stream(self.stream):
             self.graph.replay()
         self.stream.synchronize()
+        self.emu.net.check_status(int(self.h_status[0]))
         out = self.h_out_np[:, :q, :self.emu.n_out].astype(np.float64) * self.emu.sd + self.emu.mu
         return out.mean(axis=0).reshape(q, self.emu.nfreqs, 4)
 

@@ -114,9 +114,53 @@ def reduce_stats(stats, device=None):
     return out
 
 
-def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=None):
+#: per-sample file name in a library's output directory (librarian/__init__.py:56)
+FNAME_LIBRARY_SIM_FILE = "library__p{pnum:06d}.npz"
+
+
+def sim_fname(output_dir, index):
+    """Path of sample ``index``'s file in ``output_dir`` (lib_tools.py:1018-1026)."""
+    return os.path.join(str(output_dir), FNAME_LIBRARY_SIM_FILE.format(pnum=int(index)))
+
+
+def load_sim_file(path):
+    """A sample file's contents as a dict, or None when the file records a failure (a 'fail' key) or
+    cannot be read; list-valued keys written from lists come back as arrays."""
+    try:
+        with np.load(path, allow_pickle=False) as z:
+            if "fail" in z.files:
+                return None
+            return {kk: z[kk] for kk in z.files}
+    except (OSError, ValueError):
+        return None
+
+
+def _save_sim_file(path, space, job, res, err):
+    """Write a sample's result (with its parameters, as gen_lib.py:313-315 adds them) or, for a failed
+    sample, a file holding only 'fail' (gen_lib.py:316-323).  The file appears under its final name
+    only once complete."""
+    if err is not None:
+        data = dict(fail=str(err))
+    else:
+        data = {kk: vv for kk, vv in res.items() if not isinstance(vv, list)}
+        for kk, vv in res.items():
+            if isinstance(vv, list):
+                for ii, arr in enumerate(vv):
+                    data[f"{kk}_{ii}"] = arr
+        data["params"] = np.array([job.params[pn] for pn in space.param_names])
+        data["param_names"] = np.array(space.param_names)
+    tmp = path + ".part.npz"
+    np.savez(tmp, **data)
+    os.replace(tmp, path)
+
+
+def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=None, output_dir=None,
+              max_failures=None):
     """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: result or None}
-    and {index: exception} for samples that failed.  A result is run_model's dict, or ``reduce`` of it."""
+    and {index: exception} for samples that failed.  A result is run_model's dict, or ``reduce`` of it.
+    With ``output_dir`` every sample also writes its file there as it finishes.  With ``max_failures``
+    the workers stop taking samples once more than that many have failed, and RuntimeError is raised
+    (gen_lib.py:213-218)."""
     t = D.torch()
     dev = D.device()
     order = sorted(jobs, key=lambda j: -j.cost(nfreqs))
@@ -124,23 +168,35 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
     for job in order:
         q.put(job)
     results, errors = {}, {}
+    lock = threading.Lock()
+    stop = threading.Event()
     streams = [t.cuda.Stream(device=dev) for _ in range(workers)]
 
     def work(stream):
         with t.cuda.stream(stream):
-            while True:
+            while not stop.is_set():
                 try:
                     job = q.get_nowait()
                 except queue.Empty:
                     return
+                res = err = None
                 try:
                     sam, hard = space.model_for_params(job.params, job.shape)
                     res = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
                                     nloudest=nloudest, seed=job.seed, **flags)
-                    results[job.index] = res if reduce is None else reduce(res)
-                except Exception as err:   # a failed sample gives NaN rows, as in the reference's libraries
-                    results[job.index] = None
-                    errors[job.index] = err
+                except Exception as exc:   # a failed sample gives NaN rows, as in the reference's libraries
+                    err = exc
+                if output_dir is not None:
+                    try:
+                        _save_sim_file(sim_fname(output_dir, job.index), space, job, res, err)
+                    except OSError as exc:
+                        err = err or exc
+                with lock:
+                    results[job.index] = None if err is not None else (res if reduce is None else reduce(res))
+                    if err is not None:
+                        errors[job.index] = err
+                        if max_failures is not None and len(errors) > max_failures:
+                            stop.set()
 
     threads = [threading.Thread(target=work, args=(s,), daemon=True) for s in streams]
     for th in threads:
@@ -149,6 +205,10 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
         th.join()
     for s in streams:
         s.synchronize()
+    if stop.is_set():
+        first = min(errors)
+        raise RuntimeError(f"{len(errors)} library samples failed, more than max_failures={max_failures}; "
+                           f"first: sample {first}: {errors[first]!r}") from errors[first]
     if errors and len(errors) == len(jobs):
         raise next(iter(errors.values()))
     return results, errors
@@ -227,7 +287,8 @@ def autotune(space, jobs, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST, pta_du
 
 def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST,
                 pta_dur=DEF_PTA_DUR, seed=0, singles_flag=True, gwb_flag=False, params_flag=False,
-                details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None, reduce=None):
+                details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None, reduce=None,
+                output_dir=None, recreate=False, max_failures=None):
     """Evaluate the samples of ``space`` (all, or ``indices``) on this GPU; returns the list of
     per-sample :func:`lib_tools.run_model` dicts in sample order (``None`` for a failed sample), the
     input that :func:`lib_tools.write_library` takes.
@@ -238,11 +299,36 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     ``stats``, when a dict, receives the schedule, wall time, sample count, realizations and draws.
     ``reduce``, when given, maps each sample's dict to what is kept (on the worker, as soon as the
     sample is done), so large libraries need not hold every realization in host memory.
+
+    ``output_dir``: every sample writes ``library__p{index:06d}.npz`` there as it finishes (its
+    run_model dict plus ``params`` / ``param_names``; list-valued keys as ``key_0``, ``key_1``, ...), or
+    a file holding only ``fail`` when it fails (gen_lib.py:236-323).  A rerun resumes: samples whose
+    file exists and is not a failure are loaded instead of run (unless ``recreate``), failed ones are
+    attempted again (gen_lib.py:288-300).  ``max_failures``: raise RuntimeError once more samples than
+    this have failed (gen_lib.py:42, :213-218).
     """
     flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag)
     jobs = make_jobs(space, shapes, nreals, seed, indices)
+    done = {}
+    if output_dir is not None:
+        os.makedirs(str(output_dir), exist_ok=True)
+        if not recreate:
+            for job in jobs:
+                path = sim_fname(output_dir, job.index)
+                if os.path.exists(path):
+                    res = load_sim_file(path)
+                    if res is not None:
+                        done[job.index] = res if reduce is None else reduce(res)
+        jobs_all, jobs = jobs, [j for j in jobs if j.index not in done]
+    else:
+        jobs_all = jobs
+    if stats is not None:
+        stats.update(skipped=len(done))
     if not jobs:
-        return []
+        if stats is not None:
+            stats.update(workers=0, waves=None, seconds=0.0, samples=len(jobs_all), failed=0, realizations=0,
+                         draws=0.0, tuning=None, errors={})
+        return [done.get(j.index) for j in sorted(jobs_all, key=lambda j: j.index)]
     tuned = None
     if workers is None or waves is None:
         if tune:
@@ -258,14 +344,16 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     try:
         D.torch().cuda.synchronize()
         t0 = time.perf_counter()
-        results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags, reduce)
+        results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags, reduce,
+                                    output_dir=output_dir, max_failures=max_failures)
         D.torch().cuda.synchronize()
         wall = time.perf_counter() - t0
     finally:
         N.check(lib.hgb_set_bulk_waves(old_waves), "hgb_set_bulk_waves")
     if stats is not None:
-        stats.update(workers=int(workers), waves=int(waves), seconds=wall, samples=len(jobs),
+        stats.update(workers=int(workers), waves=int(waves), seconds=wall, samples=len(jobs_all),
                      failed=len(errors), realizations=int(sum(j.nreals for j in jobs)),
                      draws=float(sum(j.cost(nfreqs) for j in jobs)), tuning=tuned,
                      errors={k: repr(v) for k, v in errors.items()})
-    return [results.get(j.index) for j in sorted(jobs, key=lambda j: j.index)]
+    results.update(done)
+    return [results.get(j.index) for j in sorted(jobs_all, key=lambda j: j.index)]

@@ -110,15 +110,24 @@ def clear_plan_cache():
         _PLANS.clear()
 
 
-def add_scatter_to_masses_device(mtot, mrat, dens, scatter, refine=4):
-    """Scatter the device density tensor ``dens`` (M, Q, Z) in place."""
+def add_scatter_to_masses_device(mtot, mrat, dens, scatter, refine=4, tol=GRAD_TOL, maxiter=GRAD_MAXITER):
+    """Scatter the device density tensor ``dens`` (M, Q, Z) in place.  ``tol`` / ``maxiter`` are the
+    gradient solve's stopping rule and sweep limit (CloughTocher2DInterpolator's arguments of those
+    names; the reference uses their defaults).  Running out of sweeps warns, as scipy does."""
     plan = device_plan(mtot, mrat, scatter, refine)
+    struct = plan.struct
+    if tol != GRAD_TOL or maxiter != GRAD_MAXITER:
+        if not (tol > 0.0 and int(maxiter) >= 1):
+            raise ValueError(f"tol must be > 0 and maxiter >= 1, got {tol=} {maxiter=}")
+        struct = N.HgbScatterPlan.from_buffer_copy(plan.struct)   # the cached plan stays as built
+        struct.grad_tol = float(tol)
+        struct.grad_maxiter = int(maxiter)
     nz = int(dens.shape[2])
     lib = N.load()
     ws_bytes = lib.hgb_scatter_workspace_bytes(plan.struct.n_mtot, plan.struct.n_mrat, nz, plan.sizes.n_grid)
     ws = D.workspace(ws_bytes, dens.device)
     st = D.StatusWord(dens.device)
-    N.call("hgb_add_scatter_to_masses", ctypes.byref(plan.struct), N.ptr(dens), nz, N.ptr(ws), int(ws_bytes), st.ptr,
+    N.call("hgb_add_scatter_to_masses", ctypes.byref(struct), N.ptr(dens), nz, N.ptr(ws), int(ws_bytes), st.ptr,
            N.stream_handle())
     code = st.read()
     if code & N.STATUS_GRADIENT_NOT_CONVERGED:
@@ -126,11 +135,12 @@ def add_scatter_to_masses_device(mtot, mrat, dens, scatter, refine=4):
     return dens
 
 
-def add_scatter_to_masses(mtot, mrat, dens, scatter, refine=4, log=None):
-    """Same arguments and result as holodeck.sams.sam.add_scatter_to_masses (numpy in, numpy out)."""
+def add_scatter_to_masses(mtot, mrat, dens, scatter, refine=4, log=None, tol=GRAD_TOL, maxiter=GRAD_MAXITER):
+    """Same arguments and result as holodeck.sams.sam.add_scatter_to_masses (numpy in, numpy out);
+    ``tol`` / ``maxiter`` as in :func:`add_scatter_to_masses_device`."""
     assert np.ndim(dens) == 3
     assert np.shape(dens)[:2] == (np.size(mtot), np.size(mrat))
     like_torch = D.is_torch(dens)
     out = D.as_device(dens).clone()
-    add_scatter_to_masses_device(mtot, mrat, out, scatter, refine)
+    add_scatter_to_masses_device(mtot, mrat, out, scatter, refine, tol=tol, maxiter=maxiter)
     return out if like_torch else D.to_host(out)

@@ -36,7 +36,7 @@ def ss_realize_device(number, h2fdf, realize, loudest, seed=None, replay=None, o
     if order is None:
         order = sort_order_device(h2fdf)
     else:
-        order = D.as_device(order, dtype=D.torch().int32)
+        order = cyutils.checked_order(order, h2fdf.numel() // h2fdf.shape[-1], h2fdf.device)
     st = D.StatusWord(number.device)
     hc2ss, hc2bg = cyutils.loudest_device(num, hh, int(realize), int(loudest), order, seed=seed, replay=replay,
                                           status=st)
@@ -70,7 +70,7 @@ def ss_params_device(edges, redz, number, h2fdf, realize, loudest, seed=None, re
     if order is None:
         order = sort_order_device(h2fdf)
     else:
-        order = D.as_device(order, dtype=D.torch().int32)
+        order = cyutils.checked_order(order, h2fdf.numel() // h2fdf.shape[-1], h2fdf.device)
     host = [np.asarray(D.to_host(e) if D.is_torch(e) else e, dtype=np.float64) for e in edges[:3]]
     mt, mr, rz = (utils.midpoints(e) for e in host)
     st = D.StatusWord(number.device)

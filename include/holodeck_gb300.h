@@ -245,13 +245,19 @@ int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mt
                           const hgb_cosmo *cosmo, double *number, double *h2fdf, int *d_status, void *stream);
 
 /* order[k] = flat bin index of the k-th largest h2fdf[..., 0] (single_sources.py:89).
- * Ties keep ascending bin index. */
+ * Equal keys are put in ascending bin index.  This is a deterministic choice of this library,
+ * not the reference's behaviour: the reference orders with numpy's default (unstable) argsort,
+ * whose order among equal keys depends on the sort's partitioning.  Bins whose keys tie can
+ * therefore be visited in another order than the reference visits them; callers that must
+ * reproduce the reference's visiting order exactly pass its order to the realization entry
+ * points instead. */
 size_t hgb_sort_workspace_bytes(long n_bins);
 int hgb_argsort_f0_desc(const double *h2fdf, long n_bins, int n_freq, int32_t *order,
                         void *workspace, size_t workspace_bytes, void *stream);
 
 /* No reference counterpart.  Allocation-free variant of hgb_argsort_f0_desc for callers that
  * cannot supply a workspace: same arguments without workspace/workspace_bytes, same `order`.
+ * Equal keys are ordered as hgb_argsort_f0_desc orders them (ascending bin index).
  * Its scratch is a file-scope device array of HGB_SORT_STATIC_BYTES (24 MiB) per device, so
  * n_bins <= HGB_SORT_STATIC_MAX_BINS (2^20); larger inputs return HGB_ERR_CAPACITY with nothing
  * enqueued.  The first call on each device (with that device current) looks the array up with
@@ -270,6 +276,7 @@ int hgb_argsort_f0_desc_static(const double *h2fdf, long n_bins, int n_freq, int
  * hc2bg (F, R), both fully written.
  * mode HGB_RNG_PHILOX: draws from Philox4x32-10 keyed by seed.
  * mode HGB_RNG_REPLAY: replay[(r*F + f)*B + k] is the draw of the k-th sorted bin. */
+#define HGB_MAX_NREALS (65535L * 1024L)   /* realizations per call: 65535 grid rows of 1024 */
 size_t hgb_loudest_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode);
 int hgb_loudest_hc_from_sorted(const double *number, const double *h2fdf, long n_bins, int n_freq,
                                int nreals, int nloud, const int32_t *order, int mode, uint64_t seed,

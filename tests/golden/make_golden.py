@@ -2,7 +2,12 @@
 
 Run in a container that holds the reference sources (see ``ref_env.py``)::
 
-    python tests/golden/make_golden.py
+    HOLODECK_REF_SRC=<holodeck checkout> HOLODECK_REF_BUILD=<scratch dir> \
+        python tests/golden/make_golden.py [case_name]
+
+``case_cfg2`` (the default 91x81x101 grid) takes about two minutes of one core and ``case_cfg5`` (the
+181x161x201 grid, 100 frequencies) about half an hour and 30 GB of memory; both are summaries, so
+their fixtures stay small.
 
 Every fixture is produced by the unmodified reference code path (plus the
 one-token Cython-3 fix and import stand-ins described in ``ref_env.py``),
@@ -110,8 +115,64 @@ def case_cfg1():
         number_sum_f=number.sum(axis=(0, 1, 2)), mean_hc2_f=(number * h2fdf).sum(axis=(0, 1, 2)),
         dnum_sum_f=res["dnum"].sum(axis=(0, 1, 2)), redz_final_slice=res["redz_final"][::7, ::7, ::7, :],
         dnum_slice=res["dnum"][::7, ::7, ::7, :], order_head=res["order"][:2000],
+        # the whole visiting order: numpy's argsort orders the tied (zero) keys differently on other
+        # machines, so a replay of the reference's draws needs the reference's own order
+        order=res["order"].astype(np.int32),
     )
     save("ref_cfg1.npz", **base, **keep, norm=hard._norm, nreals=100, nloud=5, seed=0)
+
+
+def _strided(arr, step):
+    return np.ascontiguousarray(arr[::step, ::step, ::step, :])
+
+
+def case_cfg2():
+    """The default-grid workload: 91x81x101 grid, 40 frequencies, 10 loudest, with a seeded run of 2
+    realizations.  The (M, Q, Z, F) grids are kept as per-frequency sums and strided slices; the
+    loudest-first order is kept whole (int32), because numpy's argsort does not order the bins whose
+    first-frequency strain ties (the zeros), and replaying the reference's draws needs its order."""
+    sam = make_sam((91, 81, 101), 0.28)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 40)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    res = run_path(sam, hard, fobs_gw_edges, nreals=2, nloud=10, seed=0)
+    number, h2fdf, dnum, redz_final = res["number"], res["h2fdf"], res["dnum"], res["redz_final"]
+    dens = sam.static_binary_density
+    keep = dict(
+        mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, fobs_gw_edges=fobs_gw_edges, norm=hard._norm,
+        hc_ss=res["hc_ss"], hc_bg=res["hc_bg"],
+        density_slice=np.ascontiguousarray(dens[::5, ::5, ::5]),
+        number_sum_f=number.sum(axis=(0, 1, 2)), mean_hc2_f=(number * h2fdf).sum(axis=(0, 1, 2)),
+        dnum_sum_f=dnum.sum(axis=(0, 1, 2)), h2fdf_max_f=h2fdf.max(axis=(0, 1, 2)),
+        redz_final_slice=_strided(redz_final, 9), dnum_slice=_strided(dnum, 9),
+        number_slice=_strided(number, 9), h2fdf_slice=_strided(h2fdf, 9),
+        order=res["order"].astype(np.int32),
+    )
+    save("ref_cfg2.npz", **keep, nreals=2, nloud=10, seed=0)
+
+
+def case_cfg5():
+    """The high-resolution grid: 181x161x201, 100 frequencies (no realizations: 10^4 of them would take
+    the reference days).  Keeps the per-frequency expected number and mean hc^2 = sum_b number h2fdf,
+    their sums over redshift bins, and strided slices of the grids."""
+    sam = make_sam((181, 161, 201), 0.28)
+    fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 100)
+    hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
+    fobs_orb_edges = fobs_gw_edges / 2.0
+    fobs_orb_cents = 0.5 * (fobs_gw_edges[1:] + fobs_gw_edges[:-1]) / 2.0
+    redz_final, dnum = sam_cyutils.dynamic_binary_number_at_fobs(fobs_orb_cents, sam, hard, holo.cosmo)
+    edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
+    number = sam_cyutils.integrate_differential_number_3dx1d(edges, dnum)
+    keep = dict(redz_final_slice=_strided(redz_final, 17), dnum_slice=_strided(dnum, 17),
+                dnum_sum_f=dnum.sum(axis=(0, 1, 2)))
+    del dnum
+    h2fdf = gravwaves.char_strain_sq_from_bin_edges_redz(edges, redz_final)
+    del redz_final
+    w = number * h2fdf
+    keep.update(mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, fobs_gw_edges=fobs_gw_edges, norm=hard._norm,
+                number_sum_f=number.sum(axis=(0, 1, 2)), mean_hc2_f=w.sum(axis=(0, 1, 2)),
+                mean_hc2_zf=w.sum(axis=(0, 1)), number_zf=number.sum(axis=(0, 1)),
+                number_slice=_strided(number, 17), h2fdf_slice=_strided(h2fdf, 17))
+    save("ref_cfg5.npz", **keep)
 
 
 def case_scatter_shapes():

@@ -1,8 +1,11 @@
 """Build and import the holodeck reference for generating golden fixtures.
 
 This helper runs only in a development container that holds the holodeck
-sources (``HOLODECK_REF_SRC``, default ``/root/reference``).  It is not used by
-the tests: they read the committed ``.npz`` fixtures.
+sources.  Two environment variables are required: ``HOLODECK_REF_SRC``, the
+root of the holodeck source tree (it holds ``holodeck/`` and ``setup.py``),
+and ``HOLODECK_REF_BUILD``, a scratch directory outside this repository for
+the patched copy and its build.  It is not used by the tests: they read the
+committed ``.npz`` fixtures.
 
 Steps, all in a scratch directory outside the repository:
 
@@ -24,9 +27,20 @@ import shutil
 import subprocess
 import sys
 
-REF_SRC = os.environ.get("HOLODECK_REF_SRC", "/root/reference")
-BUILD_DIR = os.environ.get("HOLODECK_REF_BUILD", "/tmp/hgb_ref_build")
 REPO = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
+
+
+def _required_dir(name):
+    val = os.environ.get(name)
+    if not val:
+        raise RuntimeError(f"set {name} (see the module docstring of tests/golden/ref_env.py)")
+    return os.path.abspath(val)
+
+
+REF_SRC = _required_dir("HOLODECK_REF_SRC")
+BUILD_DIR = _required_dir("HOLODECK_REF_BUILD")
+if os.path.commonpath([BUILD_DIR, REPO]) == REPO:
+    raise RuntimeError("HOLODECK_REF_BUILD must lie outside the repository")
 
 _STUBS = {
     "cosmopy/__init__.py": '''

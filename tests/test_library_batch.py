@@ -136,3 +136,71 @@ def test_autotune_times_every_candidate(built_lib):
     assert (res["workers"], res["waves"]) in ((1, 2), (2, 1))
     assert N.load().hgb_get_bulk_waves() == before
     assert batch.autotune(space, jobs, nfreqs=4, nloudest=2, candidates=((1, 2),), probe=3)["workers"] in (1, 2)
+
+
+def test_resume_loads_finished_samples_without_running_them(tmp_path):
+    """A rerun skips every sample whose file holds a result (gen_lib.py:288-300): with all files
+    present nothing is run, so no device is needed; a failure file does not count as finished."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
+    space = PS_Classic_Phenom_Uniform(nsamples=4, seed=3)
+    jobs = batch.make_jobs(space, (12, 12, 12), 5)
+    fake = {}
+    for job in jobs:
+        res = dict(fobs_cents=np.arange(3.0), fobs_edges=np.arange(4.0), hc_ss=np.full((3, 5, 2), job.index + 1.0),
+                   hc_bg=np.full((3, 5), job.index + 0.5))
+        batch._save_sim_file(batch.sim_fname(tmp_path, job.index), space, job, res, None)
+        fake[job.index] = res
+    stats = {}
+    out = batch.run_library(space, (12, 12, 12), 5, nfreqs=3, nloudest=2, output_dir=tmp_path, stats=stats)
+    assert stats["skipped"] == 4 and stats["failed"] == 0 and stats["realizations"] == 0
+    for ii, res in enumerate(out):
+        assert np.array_equal(res["hc_ss"], fake[ii]["hc_ss"]) and np.array_equal(res["hc_bg"], fake[ii]["hc_bg"])
+        assert np.array_equal(res["params"], [space.param_dict(ii)[pn] for pn in space.param_names])
+    batch._save_sim_file(batch.sim_fname(tmp_path, 9), space, jobs[0], None, RuntimeError("boom"))
+    assert batch.load_sim_file(batch.sim_fname(tmp_path, 9)) is None
+    with np.load(batch.sim_fname(tmp_path, 9)) as z:
+        assert list(z.files) == ["fail"] and "boom" in str(z["fail"])
+
+
+class _FailingSpace:
+    """A parameter space whose model for one sample raises (a host-side injected failure)."""
+
+    def __init__(self, space, bad):
+        self._space, self._bad = space, bad
+
+    def __getattr__(self, name):
+        return getattr(self._space, name)
+
+    def model_for_params(self, params, sam_shape=None):
+        if params == self._space.param_dict(self._bad):
+            raise RuntimeError("injected failure")
+        return self._space.model_for_params(params, sam_shape)
+
+
+@pytest.mark.gpu
+def test_failed_sample_is_isolated_and_resumed(built_lib, tmp_path):
+    """An exception in one sample marks that sample failed (a 'fail' file, None result, NaN rows in
+    the written library) and leaves the others intact; a rerun runs only the failed sample; more
+    failures than max_failures raise."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch, lib_tools
+    space = PS_Classic_Phenom_Uniform(nsamples=5, seed=2)
+    shapes, _ = batch.random_shapes(5, lo=10, hi=14, seed=8)
+    nreals = [7] * 5     # one realization count, as a combined library file holds
+    kw = dict(nfreqs=4, nloudest=2, seed=13, workers=2, waves=2)
+    stats = {}
+    out = batch.run_library(_FailingSpace(space, 2), shapes, nreals, output_dir=tmp_path, stats=stats, **kw)
+    assert stats["failed"] == 1 and 2 in stats["errors"] and out[2] is None
+    assert batch.load_sim_file(batch.sim_fname(tmp_path, 2)) is None
+    clean = batch.run_library(space, shapes, nreals, **kw)
+    for ii in (0, 1, 3, 4):
+        assert np.array_equal(out[ii]["hc_ss"], clean[ii]["hc_ss"]) and np.array_equal(out[ii]["hc_bg"], clean[ii]["hc_bg"])
+    lib = lib_tools.write_library(str(tmp_path / "lib.npz"), out, space.param_samples, space.param_names)
+    with np.load(lib) as z:
+        assert np.all(np.isnan(z["hc_bg"][2])) and np.all(np.isnan(z["sample_params"][2]))
+        assert np.all(np.isfinite(z["hc_bg"][[0, 1, 3, 4]]))
+    stats = {}
+    again = batch.run_library(space, shapes, nreals, output_dir=tmp_path, stats=stats, **kw)
+    assert stats["skipped"] == 4 and stats["failed"] == 0 and stats["realizations"] == nreals[2]
+    assert np.array_equal(again[2]["hc_ss"], clean[2]["hc_ss"]) and np.array_equal(again[2]["hc_bg"], clean[2]["hc_bg"])
+    with pytest.raises(RuntimeError, match="max_failures"):
+        batch.run_library(_FailingSpace(space, 1), shapes, nreals, max_failures=0, **kw)
