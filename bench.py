@@ -147,8 +147,9 @@ def run_gpu(args):
     def step(i, keep_on_device=True):
         sam, hard = make_model(H, C)
         if keep_on_device:
-            return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i, return_torch=True)
-        return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i)
+            return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i, return_torch=True,
+                           precision=args.precision)
+        return sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=seed0 + i, precision=args.precision)
 
     for i in range(args.warmup):
         step(i)
@@ -185,14 +186,16 @@ def run_gpu(args):
     # the reference caches static_binary_density); dbn, integration, strain, sort and realizations
     # recomputed every step
     warm_sam, warm_hard = make_model(H, C)
-    warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0, return_torch=True)
+    warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0, return_torch=True,
+                 precision=args.precision)
     barrier()
     w0 = torch.cuda.Event(enable_timing=True)
     w1 = torch.cuda.Event(enable_timing=True)
     w0.record()
     for i in range(args.steps):
         flush.zero_()
-        warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0 + 7919 + i, return_torch=True)
+        warm_sam.gwb(fe, hard=warm_hard, realize=NREALS, loudest=NLOUD, seed=seed0 + 7919 + i, return_torch=True,
+                     precision=args.precision)
     w1.record()
     barrier()
     warm_ms = w0.elapsed_time(w1) / args.steps
@@ -568,9 +571,10 @@ def run_profile(args):
     fe = fe[:args.nfreqs + 1]
     for i in range(args.warmup + 1):
         sam, hard = make_model(H, C)
-        sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=i, return_torch=True)
+        sam.gwb(fe, hard=hard, realize=NREALS, loudest=NLOUD, seed=i, return_torch=True, precision=args.precision)
     torch.cuda.synchronize()
-    print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1}))
+    print(json.dumps({"profile": CONFIG_NAME, "nfreqs": args.nfreqs, "evaluations": args.warmup + 1,
+                      "precision": args.precision}))
 
 
 HIRES_SHAPE = (181, 161, 201)
@@ -671,9 +675,9 @@ def run_stages(args):
         ev[1].record()
         hard._norm_device()
         ev[2].record()
-        redz_final, diff_num = sam._dbn_device(hard, fo_c)
+        redz_final, diff_num = sam._dbn_device(hard, fo_c, precision=args.precision)
         ev[3].record()
-        number, h2fdf = sam._number_and_strain(fe / 2.0, diff_num, redz_final)
+        number, h2fdf = sam._number_and_strain(fe / 2.0, diff_num, redz_final, precision=args.precision)
         ev[4].record()
         order = single_sources.sort_order_device(h2fdf)
         ev[5].record()
@@ -684,7 +688,7 @@ def run_stages(args):
             rows.append([ev[k].elapsed_time(ev[k + 1]) for k in range(len(names))])
     med = [statistics.median(r[k] for r in rows) for k in range(len(names))]
     print(json.dumps({"stages_ms": dict(zip(names, [round(m, 3) for m in med])), "sum_ms": round(sum(med), 3),
-                      "config": {"workload": CONFIG_NAME}, "evaluations": args.steps}))
+                      "config": {"workload": CONFIG_NAME, "precision": args.precision}, "evaluations": args.steps}))
 
 
 def main():
@@ -693,6 +697,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"],
+                    help="grid arithmetic of the timed steps (fp32: the production mode; fp64: the parity mode)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="run warmup + 1 untimed evaluations (for ncu)")
     ap.add_argument("--nfreqs", type=int, default=NFREQ, help="frequencies of a --profile run")

@@ -80,6 +80,23 @@ def comoving_distance_table(cosmo, n=_DC_TABLE_N):
     return val, der
 
 
+def distance_ratio_table(cosmo, val, der, n=_DC_TABLE_N):
+    """The FP32 entry points' distance table: g(u) = D_C(u) / (D_H (1 - u)) and dg/du on u = k/n, from
+    the FP64 values and derivatives of :func:`comoving_distance_table`.  At u = 1 (z = 0) g is the
+    limit -D_C'(1) / D_H = 2 / sqrt(Om0 + Ode0) and dg/du = -D_C''(1) / (2 D_H) = -3 Ode0 (Om0 + Ode0)^(-3/2)."""
+    uu = np.arange(n + 1, dtype=np.float64) / n
+    w = 1.0 - uu
+    dh = cosmo.hubble_distance
+    g = np.empty(n + 1)
+    dg = np.empty(n + 1)
+    g[:n] = val[:n] / (dh * w[:n])
+    dg[:n] = (der[:n] * w[:n] + val[:n]) / (dh * w[:n] ** 2)
+    s = cosmo.Om0 + cosmo.Ode0
+    g[n] = 2.0 / np.sqrt(s)
+    dg[n] = -3.0 * cosmo.Ode0 * s ** -1.5
+    return g.astype(np.float32), dg.astype(np.float32)
+
+
 class DeviceCosmology:
     """Device copies of a :class:`holodeck_gb300.cosmology.Cosmology` and its ``hgb_cosmo`` struct."""
 
@@ -91,6 +108,10 @@ class DeviceCosmology:
         val, der = comoving_distance_table(cosmo)
         self.dc_val = as_device(val, dev)
         self.dc_der = as_device(der, dev)
+        gv, gd = distance_ratio_table(cosmo, val, der)
+        t = torch()
+        self.dcg_val = as_device(gv, dev, dtype=t.float32)
+        self.dcg_der = as_device(gd, dev, dtype=t.float32)
         s = N.HgbCosmo()
         s.H0 = cosmo.H0
         s.Om0 = cosmo.Om0
@@ -107,6 +128,8 @@ class DeviceCosmology:
         s.dc_val = N.ptr(self.dc_val)
         s.dc_der = N.ptr(self.dc_der)
         s.dc_n = _DC_TABLE_N
+        s.dcg_val = N.ptr(self.dcg_val)
+        s.dcg_der = N.ptr(self.dcg_der)
         self.struct = s
 
     @property

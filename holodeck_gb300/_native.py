@@ -49,7 +49,7 @@ class HgbCosmo(ctypes.Structure):
         ("H0", _d), ("Om0", _d), ("Ode0", _d), ("age_pref", _d), ("age_c1", _d), ("tz_c2", _d),
         ("age_limit", _d), ("hubble_distance", _d),
         ("grid_z", _p), ("grid_age", _p), ("grid_dcom", _p), ("grid_size", _i),
-        ("dc_val", _p), ("dc_der", _p), ("dc_n", _i),
+        ("dc_val", _p), ("dc_der", _p), ("dc_n", _i), ("dcg_val", _p), ("dcg_der", _p),
     ]
 
 
@@ -108,11 +108,15 @@ SIGNATURES = [
                           ctypes.POINTER(HgbCosmo), _p, _p, _p]),
     ("hgb_dbn_2pwl_phase", _i, [_p, _i, _i, _d, _i, _p, _d, _d, _d, _p, _p, _i, _p, _i, _p, _i, _p,
                                 ctypes.POINTER(HgbCosmo), _p, _p, _i, _p]),
+    ("hgb_dbn_2pwl_phase_f32", _i, [_p, _i, _i, _d, _i, _p, _d, _d, _d, _p, _p, _i, _p, _i, _p, _i, _p,
+                                    ctypes.POINTER(HgbCosmo), _p, _p, _i, _p]),
     ("hgb_dbn_gw", _i, [_p, _i, _p, _p, _i, _p, _i, _i, _p, ctypes.POINTER(HgbCosmo), _p, _p, _p]),
     ("hgb_integrate_3dx1d", _i, [_p, _i, _p, _i, _p, _i, _p, _i, _p, _p, _p]),
     ("hgb_char_strain_sq", _i, [_p, _i, _p, _i, _i, _p, _i, _p, _d, ctypes.POINTER(HgbCosmo), _p, _p, _p]),
     ("hgb_number_and_strain", _i, [_p, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _d, ctypes.POINTER(HgbCosmo),
                                    _p, _p, _p, _p]),
+    ("hgb_number_and_strain_f32", _i, [_p, _p, _i, _p, _i, _p, _i, _p, _p, _i, _p, _p, _d, ctypes.POINTER(HgbCosmo),
+                                       _p, _p, _p, _p]),
     ("hgb_sort_workspace_bytes", _sz, [_l]),
     ("hgb_argsort_f0_desc", _i, [_p, _l, _i, _p, _p, _sz, _p]),
     ("hgb_argsort_f0_desc_static", _i, [_p, _l, _i, _p, _p]),
@@ -190,8 +194,8 @@ def check(rc, what):
 #: per 8 key bits); used to report the launch count of a timed region
 KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
-    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_gw": 1,
-    "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_argsort_f0_desc": 11,
+    "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_2pwl_phase_f32": 1, "hgb_dbn_gw": 1,
+    "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_number_and_strain_f32": 1, "hgb_argsort_f0_desc": 11,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
     "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1,
 }

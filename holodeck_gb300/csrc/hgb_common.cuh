@@ -112,6 +112,52 @@ __device__ __forceinline__ double comoving_distance_fast(const double *dval, con
     return h00 * dval[k] + h10 * h * dder[k] + h01 * dval[k + 1] + h11 * h * dder[k + 1];
 }
 
+// ---- FP32-mode helpers.  On this GPU an FP64 instruction costs a warp about as much issue time as
+// 32 FP32 ones, so the FP32 kernels move values between the FP64 arrays of the API and FP32
+// registers with integer operations instead of FP64 conversions.
+
+// x rounded toward zero to float; |x| below FLT_MIN gives a signed zero, beyond FLT_MAX +-inf
+// (NaN stays NaN).  Relative error below 2^-23.
+__device__ __forceinline__ float f64_to_f32_rz(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const int ex = (int)((hi >> 20) & 0x7FFu);
+    const int e = ex - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (ex == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (((hi & 0xFFFFFu) | lo) ? 0x400000u : 0u));
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
+}
+
+// v * 2^k as a double, exactly, for a float v that is zero, normal, inf or NaN (a subnormal v gives
+// a signed zero); |k| must keep the result inside the double range.
+__device__ __forceinline__ double f32_to_f64_scaled(float v, int k) {
+    const unsigned u = __float_as_uint(v);
+    const unsigned sign = u & 0x80000000u;
+    const int ef = (int)((u >> 23) & 0xFFu);
+    if (ef == 0) return __longlong_as_double((long long)((unsigned long long)sign << 32));
+    unsigned hi;
+    if (ef == 0xFF) hi = sign | 0x7FF00000u | ((u & 0x7FFFFFu) ? 0x80000u : 0u);
+    else hi = sign | ((unsigned)(ef - 127 + 1023 + k) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const unsigned lo = (u & 0x7u) << 29;
+    return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+
+// the bit pattern of -1.0, the "no target reached" sentinel of redz_final
+constexpr long long F64_MINUS_ONE_BITS = (long long)0xBFF0000000000000ull;
+
+// Kahan-compensated FP32 accumulator
+struct Kahan32 {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
 __host__ __device__ __forceinline__ long ceil_div(long a, long b) { return (a + b - 1) / b; }
 
 // Multiprocessor count of the current device (queried once per device, 152 on a GB300).

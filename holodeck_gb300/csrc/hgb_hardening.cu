@@ -452,6 +452,112 @@ __global__ void k_dbn_2pwl_eval(CyConst cc, Dbn2plArgs a, const double *__restri
     }
 }
 
+// ---- FP32 production mode of k_dbn_2pwl_eval
+//
+// The age -> redshift inversion (bracket, interpolated redshift and comoving distance) stays FP64, as
+// in the reference; the residence time and the cosmological factor are FP32.  FP64 work per element:
+// the bracket offset, two interpolations and the two products with the density.  The age bracket
+// compares the positive FP64 ages as integers (IEEE order of positive doubles), off the FP64 pipe.
+// Ranges: the hardening rate is -(A P(x) + G / x^3) with x = sepa / rchar, A = norm and
+// G = |GW_DADT_SEP_CONST| mt^3 mr / (1 + mr)^2 / rchar^3 per cell; both constants are scaled by the
+// same power of two 2^-e0 (e0 the larger exponent), so the sum is a normal float wherever either term
+// matters, and the residence time comes out as t_s 2^-e0.
+
+// x^y for the planned exponents in FP32 (as pow_planned / pow_ratio_planned)
+__device__ __forceinline__ float pow_planned_f32(float x, float y, PowPlan p) {
+    if (p.kind == 0) return powf(x, y);
+    float r = (p.kind == 2) ? sqrtf(x) : 1.0f;
+    for (int i = 0; i < p.n; i++) r *= x;
+    return p.neg ? __fdividef(1.0f, r) : r;
+}
+
+__device__ __forceinline__ int while_while_increasing_bits(int start, int size, double val, const double *edges) {
+    const long long v = __double_as_longlong(val);   // val and edges are positive: integer order is IEEE order
+    int index = start;
+    while ((index < size - 2) && (__double_as_longlong(edges[index + 1]) < v)) index += 1;
+    while ((index > 0) && (__double_as_longlong(edges[index]) > v)) index -= 1;
+    return index;
+}
+
+__global__ void k_dbn_2pwl_eval_f32(CyConst cc, Dbn2plArgs a, const double *__restrict__ fobs,
+                                    const double *__restrict__ hard_norm, const double *__restrict__ nden,
+                                    const double *__restrict__ mtot, const double *__restrict__ mrat,
+                                    const double *__restrict__ zgrid_g, const double *__restrict__ agrid_g,
+                                    const double *__restrict__ dgrid_g, double *__restrict__ redz_final,
+                                    double *__restrict__ diff_num) {
+    extern __shared__ double smem[];
+    const int NI = a.n_interp, NF = a.n_freq;
+    double *zg = smem;
+    double *ag = zg + NI;
+    double *dg = ag + NI;
+    double *sz = dg + NI;            // [NI] dz/dt and d(d_C)/dt of each age-table interval
+    double *sd = sz + NI;
+    float *ft = (float *)(sd + NI);  // [NF]
+    const int cell = blockIdx.x;
+    const int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
+    for (int i = threadIdx.x; i < NI; i += blockDim.x) {
+        zg[i] = zgrid_g[i];
+        ag[i] = agrid_g[i];
+        dg[i] = dgrid_g[i];
+    }
+    for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = hgb::f64_to_f32_rz(fobs[i]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < NI - 1; i += blockDim.x) {
+        const double dt = ag[i + 1] - ag[i];
+        sz[i] = (zg[i + 1] - zg[i]) / dt;
+        sd[i] = (dg[i + 1] - dg[i]) / dt;
+    }
+    __shared__ float s_k13, s_as, s_gs, s_rchar_inv;
+    __shared__ int s_e0;
+    if (threadIdx.x == 0) {
+        const double mt = mtot[ii], mr = mrat[jj], norm = hard_norm[cell];
+        const double gc = fabs(cc.c_dadt) * pow(mt, 3.0) * mr / pow(1.0 + mr, 2.0) / pow(a.rchar, 3.0);
+        int ea = -100000, eg = -100000;
+        if (norm > 0.0) frexp(norm, &ea);
+        if (gc > 0.0) frexp(gc, &eg);
+        const int e0 = ea > eg ? ea : eg;
+        s_e0 = e0;
+        s_as = (float)ldexp(norm, -e0);   // in [0.5, 1) or flushed to 0 when negligible
+        s_gs = (float)ldexp(gc, -e0);
+        s_k13 = (float)(cc.ksepa * pow(mt, 1.0 / 3.0));
+        s_rchar_inv = (float)(1.0 / a.rchar);
+    }
+    __syncthreads();
+    const float k13 = s_k13, as = s_as, gs = s_gs, rchar_inv = s_rchar_inv;
+    const int e0 = s_e0;
+    const float fourpi = (float)cc.fourpi, inv_mpc = (float)(1.0 / HGB_CY_MPC);
+    const long nzf = (long)a.n_redz * NF;
+    const long base = (long)cell * nzf;
+    for (long e = threadIdx.x; e < nzf; e += blockDim.x) {
+        const double hint = redz_final[base + e];
+        if (__double_as_longlong(hint) < 0) continue;   // no bracket (-1): stays -1 / 0
+        const int f = (int)(e % NF);
+        const int kk = (int)(e / NF);
+        const double new_time = diff_num[base + e];
+        const int ni = while_while_increasing_bits((int)hint, NI, new_time, ag);
+        const double dt = new_time - ag[ni];
+        const double new_redz = zg[ni] + dt * sz[ni];
+        const double dcom = dg[ni] + dt * sd[ni];
+        const float zp1 = 1.0f + hgb::f64_to_f32_rz(new_redz);
+        const float frst = ft[f] * zp1;
+        const float r = rcbrtf(frst);
+        const float sp = k13 * (r * r);
+        const float xx = sp * rchar_inv;
+        const float pw = (a.p_outer.kind && a.p_inner.kind)
+                             ? pow_planned_f32(1.0f + xx, (float)(-a.go + a.gi), a.p_outer) *
+                                   pow_planned_f32(xx, (float)(1.0 - a.gi), PowPlan{a.p_inner.kind, a.p_inner.n,
+                                                                                   !a.p_inner.neg})
+                             : __fdividef(powf(1.0f + xx, (float)(-a.go + a.gi)), powf(xx, (float)(a.gi - 1.0)));
+        const float rate = fmaf(as, pw, __fdividef(gs, xx * xx * xx));
+        const float tres = __fdividef((2.0f / 3.0f) * sp, rate);        // residence time 2^e0
+        const float dcm = hgb::f64_to_f32_rz(dcom) * inv_mpc;
+        const float cosmo_fact = fourpi * zp1 * (dcm * dcm);
+        redz_final[base + e] = new_redz;
+        diff_num[base + e] = nden[(long)cell * a.n_redz + kk] * hgb::f32_to_f64_scaled(tres, -e0) *
+                             hgb::f32_to_f64_scaled(cosmo_fact, 0);
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // differential binary number, Hard_GW
 // ------------------------------------------------------------------------------------------------
@@ -781,6 +887,36 @@ int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, doub
         return hgb::check_launch();
     }
     return HGB_OK;
+}
+
+int hgb_dbn_2pwl_phase_f32(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                           const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                           const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                           const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                           double *redz_final, double *diff_num, int phase, void *stream) {
+    HGB_CHECK_ARG(phase >= 1 && phase <= 3);
+    HGB_CHECK_ARG(fobs_orb && hard_norm && mtot && mrat && cosmo && redz_final && diff_num);
+    HGB_CHECK_ARG(!(phase & 2) || nden);
+    HGB_CHECK_ARG(n_freq > 0 && num_steps > 0 && n_mtot > 0 && n_mrat > 0 && n_redz > 0);
+    HGB_CHECK_ARG(cosmo->grid_size >= 2 && cosmo->grid_z && cosmo->grid_age && cosmo->grid_dcom);
+    HGB_CHECK_ARG(sepa_init > 0.0 && rchar > 0.0);
+    if (phase & 1) {   // the separation-step walk is the hardening integral: FP64 in both modes
+        int rc = hgb_dbn_2pwl_phase(fobs_orb, n_freq, fobs_sorted, sepa_init, num_steps, hard_norm, rchar,
+                                    gamma_inner, gamma_outer, nden, mtot, n_mtot, mrat, n_mrat, redz, n_redz,
+                                    gmt_time, cosmo, redz_final, diff_num, 1, stream);
+        if (rc) return rc;
+    }
+    if (!(phase & 2)) return HGB_OK;
+    Dbn2plArgs a{log10(sepa_init), rchar, gamma_inner, gamma_outer, num_steps, n_freq, fobs_sorted ? 1 : 0,
+                 n_mtot, n_mrat, n_redz, cosmo->grid_size, pow_plan(-gamma_outer + gamma_inner),
+                 pow_plan(gamma_inner - 1.0)};
+    unsigned blocks = (unsigned)((long)n_mtot * n_mrat);
+    size_t smem = sizeof(double) * (size_t)5 * cosmo->grid_size + sizeof(float) * (size_t)n_freq;
+    HGB_CHECK_ARG(smem <= 48 * 1024);
+    k_dbn_2pwl_eval_f32<<<blocks, 256, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden,
+                                                                     mtot, mrat, cosmo->grid_z, cosmo->grid_age,
+                                                                     cosmo->grid_dcom, redz_final, diff_num);
+    return hgb::check_launch();
 }
 
 int hgb_dbn_2pwl(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,

@@ -288,7 +288,7 @@ def autotune(space, jobs, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST, pta_du
 def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST,
                 pta_dur=DEF_PTA_DUR, seed=0, singles_flag=True, gwb_flag=False, params_flag=False,
                 details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None, reduce=None,
-                output_dir=None, recreate=False, max_failures=None):
+                output_dir=None, recreate=False, max_failures=None, precision="fp64"):
     """Evaluate the samples of ``space`` (all, or ``indices``) on this GPU; returns the list of
     per-sample :func:`lib_tools.run_model` dicts in sample order (``None`` for a failed sample), the
     input that :func:`lib_tools.write_library` takes.
@@ -305,9 +305,11 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     a file holding only ``fail`` when it fails (gen_lib.py:236-323).  A rerun resumes: samples whose
     file exists and is not a failure are loaded instead of run (unless ``recreate``), failed ones are
     attempted again (gen_lib.py:288-300).  ``max_failures``: raise RuntimeError once more samples than
-    this have failed (gen_lib.py:42, :213-218).
+    this have failed (gen_lib.py:42, :213-218).  ``precision``: the grid arithmetic of every sample
+    (see :meth:`Semi_Analytic_Model.gwb`).
     """
-    flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag)
+    flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag,
+                 precision=precision)
     jobs = make_jobs(space, shapes, nreals, seed, indices)
     done = {}
     if output_dir is not None:

@@ -219,13 +219,15 @@ def _calc_model_details(edges, redz_final, number):
 
 
 def run_model(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_NUM_REALS, nloudest=DEF_NUM_LOUDEST,
-              gwb_flag=True, singles_flag=True, details_flag=False, params_flag=False, log=None, seed=None):
+              gwb_flag=True, singles_flag=True, details_flag=False, params_flag=False, log=None, seed=None,
+              precision="fp64"):
     """One library sample (lib_tools.py:714-842): the dict a library simulation file holds.
 
     Keys: ``fobs_cents``, ``fobs_edges``; with ``details_flag`` ``static_binary_density``, ``number``,
     ``redz_final``, ``gwb_params``, ``num_params``, ``gwb_mtot_redz_final``, ``num_mtot_redz_final``;
     with ``params_flag`` ``sspar``, ``bgpar``; with ``singles_flag`` ``hc_ss``, ``hc_bg``; with
-    ``gwb_flag`` ``gwb``.  ``seed`` (added) keys the Philox draws of the realizations.
+    ``gwb_flag`` ``gwb``.  ``seed`` (added) keys the Philox draws of the realizations; ``precision``
+    (added) selects the grid arithmetic as in :meth:`Semi_Analytic_Model.gwb`.
     """
     if not any([gwb_flag, details_flag, singles_flag, params_flag]):
         err = f"No flags set!  {gwb_flag=} {details_flag=} {singles_flag=} {params_flag=}"
@@ -243,9 +245,9 @@ def run_model(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_N
         if log is not None:
             log.exception(err)
         raise RuntimeError(err)
-    redz_final, diff_num = sam._dbn_scheduled(hard, fobs_orb_cents)
+    redz_final, diff_num = sam._dbn_scheduled(hard, fobs_orb_cents, precision=precision)
     edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
-    number, h2fdf = sam._number_and_strain(fobs_orb_edges, diff_num, redz_final)
+    number, h2fdf = sam._number_and_strain(fobs_orb_edges, diff_num, redz_final, precision=precision)
     if details_flag:
         data['static_binary_density'] = sam.static_binary_density
         data['number'] = D.to_host(number)

@@ -176,7 +176,7 @@ class Semi_Analytic_Model:
 
     # ---- differential number at target frequencies (sam.py:400-466, sam_cyutils.pyx:421-504)
 
-    def _dbn_device(self, hard, fobs_orb, cosmo=None):
+    def _dbn_device(self, hard, fobs_orb, cosmo=None, precision="fp64"):
         t = D.torch()
         cosmo = self._cosmo if cosmo is None else cosmo
         dens, gmt_time, redz_prime = self._density_device()
@@ -184,14 +184,15 @@ class Semi_Analytic_Model:
         if isinstance(hard, hardening.Fixed_Time_2PL_SAM):
             if gmt_time is None:
                 gmt_time = t.zeros(self.shape, dtype=t.float64, device=dens.device)
-            return sam_cyutils.dbn_2pwl_device(fobs_orb, hard, dens, mt, mr, rz, gmt_time, cosmo=cosmo)
+            return sam_cyutils.dbn_2pwl_device(fobs_orb, hard, dens, mt, mr, rz, gmt_time, cosmo=cosmo,
+                                               precision=precision)
         if isinstance(hard, hardening.Hard_GW) or (isinstance(hard, type) and issubclass(hard, hardening.Hard_GW)):
             if redz_prime is None:
                 redz_prime = rz[None, None, :].expand(self.shape).contiguous()
             return sam_cyutils.dbn_gw_device(fobs_orb, dens, mt, mr, redz_prime, cosmo=cosmo)
         raise ValueError(f"Unexpected `hard` value {hard}!")
 
-    def _dbn_2pwl_overlapped(self, hard, fobs_orb):
+    def _dbn_2pwl_overlapped(self, hard, fobs_orb, precision="fp64"):
         """_dbn_device for Fixed_Time_2PL_SAM on a fresh instance, with the separation-step walk (which
         needs gmt_time but not the density) on a second stream while the current stream applies the
         M-Mbulge scatter; the evaluation, which needs the final density, follows on the current
@@ -215,14 +216,14 @@ class Semi_Analytic_Model:
         redz_final.record_stream(main)
         diff_num.record_stream(main)
         return sam_cyutils.dbn_2pwl_device(fobs_orb, hard, dens, mt, mr, rz, gmt_time, cosmo=self._cosmo, phase=2,
-                                           out=(redz_final, diff_num))
+                                           out=(redz_final, diff_num), precision=precision)
 
-    def _dbn_scheduled(self, hard, fobs_orb):
+    def _dbn_scheduled(self, hard, fobs_orb, precision="fp64"):
         """_dbn_device, overlapping the separation-step walk with the scatter where that applies."""
         if (self._density_t is None and self._gmt is not None and isinstance(hard, hardening.Fixed_Time_2PL_SAM)
                 and self._mmbulge._scatter_dex > 0.0):
-            return self._dbn_2pwl_overlapped(hard, fobs_orb)
-        return self._dbn_device(hard, fobs_orb)
+            return self._dbn_2pwl_overlapped(hard, fobs_orb, precision=precision)
+        return self._dbn_device(hard, fobs_orb, precision=precision)
 
     def dynamic_binary_number_at_fobs(self, hard, fobs_orb, use_cython=True, **kwargs):
         """(grid, dnum, redz_final) like sam.py:400-466 (``use_cython`` is accepted and ignored)."""
@@ -233,9 +234,10 @@ class Semi_Analytic_Model:
     # ---- GWB (sam.py:872-947)
 
     def gwb_device(self, fobs_gw_edges, hard=None, realize=100, loudest=1, seed=None, replay=None, order=None,
-                   params=False):
+                   params=False, precision="fp64"):
         """Device (hc_ss[F, R, L], hc_bg[F, R]) tensors, plus (sspar, bgpar) with ``params``; see :meth:`gwb`."""
         hard = hardening.Hard_GW() if hard is None else hard
+        sam_cyutils.check_precision(precision)
         if not isinstance(hard, (hardening.Fixed_Time_2PL_SAM, hardening.Hard_GW)):
             raise ValueError("`sam_cyutils` methods only work with `Fixed_Time_2PL_SAM` or `Hard_GW` hardening "
                              "models!  Use `gwb_only` for alternative classes!")
@@ -245,8 +247,8 @@ class Semi_Analytic_Model:
         fobs_gw_cents = utils.midpoints(fobs_gw_edges)
         fobs_orb_edges = fobs_gw_edges / 2.0
         fobs_orb_cents = fobs_gw_cents / 2.0
-        redz_final, diff_num = self._dbn_scheduled(hard, fobs_orb_cents)
-        number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final)
+        redz_final, diff_num = self._dbn_scheduled(hard, fobs_orb_cents, precision=precision)
+        number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final, precision=precision)
         if params:
             edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]
             return single_sources.ss_params_device(edges, redz_final, number, h2fdf, realize, loudest, seed=seed,
@@ -254,9 +256,9 @@ class Semi_Analytic_Model:
         return single_sources.ss_realize_device(number, h2fdf, realize, loudest, seed=seed, replay=replay,
                                                 order=order)
 
-    def _number_and_strain(self, fobs_orb_edges, diff_num, redz_final, status=None):
+    def _number_and_strain(self, fobs_orb_edges, diff_num, redz_final, status=None, precision="fp64"):
         """Device (number, h2fdf) on the (M-1, Q-1, Z-1, F) bins.  With ``status`` the redshift check
-        is left to the caller (no host read here)."""
+        is left to the caller (no host read here).  ``precision="fp32"``: hgb_number_and_strain_f32."""
         t = D.torch()
         mt, mr, rz = self._edges_device()
         lm = D.as_device(np.log10(self.mtot))
@@ -268,7 +270,8 @@ class Semi_Analytic_Model:
         number = t.empty((nm - 1, nq - 1, nz - 1, nf), dtype=t.float64, device=mt.device)
         h2fdf = t.empty_like(number)
         st = D.StatusWord(mt.device) if status is None else status
-        N.call("hgb_number_and_strain", N.ptr(mt), N.ptr(lm), nm, N.ptr(mr), nq, N.ptr(rz), nz, N.ptr(fe),
+        fn = "hgb_number_and_strain" if sam_cyutils.check_precision(precision) == "fp64" else "hgb_number_and_strain_f32"
+        N.call(fn, N.ptr(mt), N.ptr(lm), nm, N.ptr(mr), nq, N.ptr(rz), nz, N.ptr(fe),
                N.ptr(dlnf), nf, N.ptr(diff_num), N.ptr(redz_final), C.GW_SRC_CONST, dc.ref, N.ptr(number),
                N.ptr(h2fdf), st.ptr, N.stream_handle())
         if status is None:
@@ -276,17 +279,21 @@ class Semi_Analytic_Model:
         return number, h2fdf
 
     def gwb(self, fobs_gw_edges, hard=None, realize=100, loudest=1, params=False, seed=None, replay=None,
-            order=None, return_torch=False):
+            order=None, return_torch=False, precision="fp64"):
         """Characteristic strain of the L loudest sources (F, R, L) and of the background (F, R), and
         with ``params=True`` the loudest sources' (M, q, z, z_final) (4, F, R, L) and the background's
         weighted-mean parameters (7, F, R).
 
         Same arguments and results as sam.py:872-947.  Added keywords: ``seed`` (Philox key; default
         fresh entropy), ``replay``/``order`` (replay an externally drawn Poisson stream bit for bit),
-        ``return_torch`` (keep the results on the device).
+        ``return_torch`` (keep the results on the device), ``precision``: "fp64" (default, the parity
+        mode: every grid stage in FP64) or "fp32" (the production mode: the residence-time evaluation,
+        the cell integration and the strain in FP32 with compensated sums; the hardening integral, the
+        age -> redshift inversion and the static density stay FP64; relative error of the grids about
+        1e-6, see hgb_number_and_strain_f32 / hgb_dbn_2pwl_phase_f32).
         """
         out = self.gwb_device(fobs_gw_edges, hard=hard, realize=realize, loudest=loudest, seed=seed,
-                              replay=replay, order=order, params=params)
+                              replay=replay, order=order, params=params, precision=precision)
         if return_torch:
             return out
         return tuple(D.to_host(x) for x in out)

@@ -43,12 +43,23 @@ def dynamic_binary_number_at_fobs(fobs_orb, sam, hard, cosmo=None):
     return _out(redz_final, like_torch), _out(diff_num, like_torch)
 
 
-def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None, phase=3, out=None):
+PRECISIONS = ("fp64", "fp32")
+
+
+def check_precision(precision):
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
+    return precision
+
+
+def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None, phase=3, out=None,
+                    precision="fp64"):
     """Device arrays in, device (redz_final, diff_num) out (sam_cyutils.pyx:510-781).
 
     ``phase`` 1 runs only the separation-step walk (``dens`` may be None; the outputs then hold the
     bracketing step and time, see hgb_dbn_2pwl_phase), 2 only the evaluation into ``out`` from
-    phase 1, 3 both.
+    phase 1, 3 both.  ``precision="fp32"`` evaluates the residence time in FP32 (the walk and the
+    age -> redshift inversion stay FP64; hgb_dbn_2pwl_phase_f32).
     """
     t = D.torch()
     cosmo = _cosmo if cosmo is None else cosmo
@@ -67,7 +78,8 @@ def dbn_2pwl_device(fobs_orb, hard, dens, mtot, mrat, redz, gmt_time, cosmo=None
     else:
         redz_final, diff_num = out
     norm = D.as_device(hard._norm_device())
-    N.call("hgb_dbn_2pwl_phase", N.ptr(fo), nf, sorted_ok, float(hard._sepa_init), int(hard._num_steps),
+    fn = "hgb_dbn_2pwl_phase" if check_precision(precision) == "fp64" else "hgb_dbn_2pwl_phase_f32"
+    N.call(fn, N.ptr(fo), nf, sorted_ok, float(hard._sepa_init), int(hard._num_steps),
            N.ptr(norm), float(hard._rchar), float(hard._gamma_inner), float(hard._gamma_outer), N.ptr(dens),
            N.ptr(mtot), int(mtot.numel()), N.ptr(mrat), int(mrat.numel()), N.ptr(redz), int(redz.numel()),
            N.ptr(gmt_time), dc.ref, N.ptr(redz_final), N.ptr(diff_num), int(phase), N.stream_handle())

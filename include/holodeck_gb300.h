@@ -65,6 +65,11 @@ typedef struct {
     const double *dc_val;   /* [dc_n + 1] */
     const double *dc_der;   /* [dc_n + 1] */
     int dc_n;
+    /* the same distance for the FP32 entry points (may be NULL for the FP64 ones), written as
+     * D_C = hubble_distance (1 - u) g(u) so that it keeps its relative precision as z -> 0:
+     * g (dimensionless) and dg/du on the same nodes u = k / dc_n, cubic Hermite between them */
+    const float *dcg_val;   /* [dc_n + 1] */
+    const float *dcg_der;   /* [dc_n + 1] */
 } hgb_cosmo;
 
 /* Galaxy / black-hole population model (holodeck/sams/components.py, host_relations.py). */
@@ -216,6 +221,16 @@ int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, doub
                        const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
                        double *redz_final, double *diff_num, int phase, void *stream);
 
+/* FP32 production mode of hgb_dbn_2pwl_phase: same arguments and outputs.  Phase 1 (the
+ * separation-step walk, i.e. the hardening residence-time integral) is the FP64 walk; phase 2 keeps
+ * the age -> redshift inversion and its comoving distance in FP64 and evaluates the residence time
+ * and the cosmological factor in FP32 (relative error of diff_num about 1e-6). */
+int hgb_dbn_2pwl_phase_f32(const double *fobs_orb, int n_freq, int fobs_sorted, double sepa_init, int num_steps,
+                           const double *hard_norm, double rchar, double gamma_inner, double gamma_outer,
+                           const double *nden, const double *mtot, int n_mtot, const double *mrat, int n_mrat,
+                           const double *redz, int n_redz, const double *gmt_time, const hgb_cosmo *cosmo,
+                           double *redz_final, double *diff_num, int phase, void *stream);
+
 /* Same for Hard_GW (GW-only) hardening.  Replaces _dynamic_binary_number_at_fobs_gw,
  * sam_cyutils.pyx:788-899.  redz_prime is (M, Q, Z). */
 int hgb_dbn_gw(const double *fobs_orb, int n_freq, const double *nden, const double *mtot, int n_mtot,
@@ -243,6 +258,16 @@ int hgb_number_and_strain(const double *mtot, const double *log10_mtot, int n_mt
                           const double *redz, int n_redz, const double *fobs_orb_edges, const double *dln_freq,
                           int n_freq, const double *dnum, const double *redz_final, double gw_src_const,
                           const hgb_cosmo *cosmo, double *number, double *h2fdf, int *d_status, void *stream);
+
+/* FP32 production mode of hgb_number_and_strain: same arguments, arrays and status bits; the
+ * vertex sums run in FP32 with Kahan compensation, the strain product in FP32 with power-of-two
+ * scale factors (so nothing becomes subnormal), and only the redshift midpoints of bins whose
+ * corners mix the -1 sentinel with redshifts are formed in FP64 (the reference's midpoint cancels
+ * there).  Relative error of number and h2fdf about 1e-6.  Needs cosmo->dcg_val / dcg_der. */
+int hgb_number_and_strain_f32(const double *mtot, const double *log10_mtot, int n_mtot, const double *mrat, int n_mrat,
+                              const double *redz, int n_redz, const double *fobs_orb_edges, const double *dln_freq,
+                              int n_freq, const double *dnum, const double *redz_final, double gw_src_const,
+                              const hgb_cosmo *cosmo, double *number, double *h2fdf, int *d_status, void *stream);
 
 /* order[k] = flat bin index of the k-th largest h2fdf[..., 0] (single_sources.py:89).
  * Equal keys are put in ascending bin index.  This is a deterministic choice of this library,
