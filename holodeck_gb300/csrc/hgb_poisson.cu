@@ -89,6 +89,7 @@ constexpr int HALF_WORDS = 1536 + 1024;  // tables up to 1536 entries (2^11 u16 
 constexpr int ARENA_WORDS = 2 * HALF_WORDS;   // the halves alternate between build and draw
 static_assert(TMAX + 2048 <= ARENA_WORDS, "the largest table (2^12 guide cells) fits the whole arena");
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
+constexpr int BULK_BLOCKS_PER_SM = 6;    // k_bulk residency (seven was measured slower: 30.7 against 29.2 ms)
 constexpr unsigned GUIDE_PURE = 0x8000u, GUIDE_ONE = 0x4000u, GUIDE_M = 0x0FFFu;   // guide cell fields
 static_assert(TMAX - 1 <= (int)GUIDE_M, "table entries fit the guide's index field");
 static_assert(ARENA_WORDS >= RB * (NT + 1), "the small-lambda rows share the arena");
@@ -182,7 +183,7 @@ struct Tile {
     unsigned long long scan[NWARP];
     double lam[RB];
     float hs[RB];                     // h2fdf * 2^100 (for the background sums)
-    float b[RB], a[RB], vr[RB], log_inva[RB], frac[RB], lamf[RB], loglam[RB];
+    float frac[RB], lamf[RB];
     int lam_int[RB];
     int tb_klo[RB], tb_S[RB], tb_gb[RB];   // table kind: first count, entries, log2 guide cells
     int pos[RB];                      // sorted position (loudest) or grid index (gwb) of the bin
@@ -291,18 +292,6 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
             s.tb_S[j] = S;
             s.tb_gb[j] = 32 - __clz(S - 1);   // ceil(log2 S): 2^gb >= S guide cells, S >= 2
         }
-        if (kind == KIND_PTRS32) {
-            const float slam = sqrtf(lf);
-            const float b = 0.931f + 2.53f * slam;
-            const float a = -0.059f + 0.02483f * b;
-            const float inva = 1.1239f + 1.1328f / (b - 3.4f);
-            const float vr = 0.9277f - 3.6224f / (b - 2.0f);
-            s.b[j] = b;
-            s.a[j] = a;
-            s.vr[j] = vr;
-            s.log_inva[j] = logf(inva);
-            s.loglam[j] = logf(lf);
-        }
     }
 }
 
@@ -335,28 +324,47 @@ __device__ __forceinline__ float pmf_f32(int k, int lam_int, float frac, float l
     return expf(-bd0_f32(kk, d, lamf) - stirlerr_f32(k)) * rsqrtf(6.283185307179586f * kk);
 }
 
+// PTRS constants of one bin (Hormann 1993), formed in registers by every thread that draws it
+struct Ptrs32C {
+    float b, a, vr, log_inva, loglam, frac, lamf;
+    int lam_int;
+};
+
+__device__ __forceinline__ Ptrs32C ptrs32_consts(const Tile &s, int j) {
+    Ptrs32C p;
+    p.lamf = s.lamf[j];
+    p.frac = s.frac[j];
+    p.lam_int = s.lam_int[j];
+    const float slam = sqrtf(p.lamf);
+    p.b = 0.931f + 2.53f * slam;
+    p.a = -0.059f + 0.02483f * p.b;
+    p.vr = 0.9277f - 3.6224f / (p.b - 2.0f);
+    p.log_inva = logf(1.1239f + 1.1328f / (p.b - 3.4f));
+    p.loglam = logf(p.lamf);
+    return p;
+}
+
 // One PTRS attempt from the uniforms (U word, V word); returns k >= 0 on acceptance, -1 otherwise.
 // __logf's absolute error (< 2^-21 near 1, 3 ulp elsewhere) is far below the FP32 resolution of
 // the log-densities compared.
-__device__ __forceinline__ int ptrs32_attempt(const Tile &s, int j, uint32_t wu, uint32_t wv) {
-    const float b = s.b[j], a = s.a[j], frac = s.frac[j], lamf = s.lamf[j];
+__device__ __forceinline__ int ptrs32_attempt(const Ptrs32C &p, const float *lgam, uint32_t wu, uint32_t wv) {
     const float U = u24(wu) - 0.5f;
     const float V = u24(wv);
     const float us = 0.5f - fabsf(U);
-    const float kf = floorf((2.0f * a / us + b) * U + (frac + 0.43f));
+    const float kf = floorf((2.0f * p.a / us + p.b) * U + (p.frac + 0.43f));
     const bool in_range = (kf > -1.0e7f) && (kf < 1.0e7f) && !(us < 0.013f && V > us);
-    const int k = in_range ? s.lam_int[j] + (int)kf : -1;
+    const int k = in_range ? p.lam_int + (int)kf : -1;
     if (k < 0) return -1;
-    if (us >= 0.07f && V <= s.vr[j]) return k;
-    const float lhs = __logf(V) + s.log_inva[j] - __logf(a / (us * us) + b);
+    if (us >= 0.07f && V <= p.vr) return k;
+    const float lhs = __logf(V) + p.log_inva - __logf(p.a / (us * us) + p.b);
     float rhs;
     if (k < 16) {
-        rhs = -lamf + (float)k * s.loglam[j] - s.lgam[k];
+        rhs = -p.lamf + (float)k * p.loglam - lgam[k];
     } else {
         // log P(k; lambda) = -bd0(k, lambda) - log(2 pi k) / 2 - stirlerr(k)
         const float kk = (float)k;
-        const float d = (float)(k - s.lam_int[j]) - frac;
-        rhs = -bd0_f32(kk, d, lamf) - 0.5f * __logf(6.283185307179586f * kk) - stirlerr_f32(k);
+        const float d = (float)(k - p.lam_int) - p.frac;
+        rhs = -bd0_f32(kk, d, p.lamf) - 0.5f * __logf(6.283185307179586f * kk) - stirlerr_f32(k);
     }
     return (lhs <= rhs) ? k : -1;
 }
@@ -895,7 +903,7 @@ __device__ __forceinline__ void add_par(float *psm, int sl, int t, int j, float 
 }
 
 template <bool SORTED, bool PARAMS>
-__global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
+__global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
                                                           const double *__restrict__ h_in,
                                                           const int *__restrict__ qpos, double *__restrict__ part,
                                                           int *d_status) {
@@ -1188,6 +1196,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
             const int j = s.list[KIND_PTRS32][li];
             const int pos = s.pos[j];
             const float hs = s.hs[j];
+            const Ptrs32C pc = ptrs32_consts(s, j);
             uint4 ctr = ctr0;
             ctr.x = (uint32_t)pos;
             ctr.w |= W_PTRS;
@@ -1200,7 +1209,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
                     cc.w |= (uint32_t)(it >> 1);
                     w = philox(cc, a.key);
                 }
-                const int k = (it & 1) ? ptrs32_attempt(s, j, w.z, w.w) : ptrs32_attempt(s, j, w.x, w.y);
+                const int k = (it & 1) ? ptrs32_attempt(pc, s.lgam, w.z, w.w) : ptrs32_attempt(pc, s.lgam, w.x, w.y);
                 it++;
                 if (k >= 0) {
                     if (!check || pos >= __ldg(q_row + sl * RB)) {
@@ -1210,7 +1219,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : 6) k_bulk(BulkArgs a, ParArgs
                     sl++;
                 } else if (it >= MAX_PTRS_ITERS) {
                     hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
-                    const float kfix = floorf(s.lamf[j] + 0.5f);
+                    const float kfix = floorf(pc.lamf + 0.5f);
                     for (; sl < rpt; sl++)
                         if (!check || pos >= __ldg(q_row + sl * RB)) {
                             add_bg(st, sl, t, kfix * hs);
@@ -1554,7 +1563,8 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int n_rgroups(int nr) { return (int)hgb::ceil_div(nr, (long)RB * RPT); }
 
-// Waves of resident k_bulk blocks (six per SM) that the chunk count aims for; set by hgb_set_bulk_waves.
+// Waves of resident k_bulk blocks (BULK_BLOCKS_PER_SM per SM) that the chunk count aims for; set by
+// hgb_set_bulk_waves.
 // A block's cost depends strongly on its frequency (the lowest frequencies hold most of the
 // occupied bins), so many short blocks balance the SMs better than a few long ones: on the
 // 91x81x101 grid with 40 frequencies and 1000 realizations the kernel takes 33.9 / 31.3 / 29.9 /
@@ -1567,7 +1577,7 @@ int bulk_waves() { return g_bulk_waves.load(std::memory_order_relaxed); }
 
 int choose_nchunk(long nb, int nf, int nr, int waves) {
     long blocks = (long)n_rgroups(nr) * nf;
-    long target = (long)hgb::sm_count() * 6 * waves;
+    long target = (long)hgb::sm_count() * BULK_BLOCKS_PER_SM * waves;
     long nchunk = hgb::ceil_div(target, blocks);
     long maxc = hgb::ceil_div(nb, 8L * RB);
     if (nchunk > maxc) nchunk = maxc;

@@ -153,25 +153,35 @@ def case_cfg2():
 def case_cfg5():
     """The high-resolution grid: 181x161x201, 100 frequencies (no realizations: 10^4 of them would take
     the reference days).  Keeps the per-frequency expected number and mean hc^2 = sum_b number h2fdf,
-    their sums over redshift bins, and strided slices of the grids."""
+    their sums over redshift bins, and strided slices of the grids.  The integration and the strain
+    are element-local, so they run through the reference's functions on slabs of the mtot axis (the
+    strain function's whole-grid temporaries would need more than 64 GB); the values are the same."""
     sam = make_sam((181, 161, 201), 0.28)
     fobs_gw_cents, fobs_gw_edges = holo.utils.pta_freqs(16.0 * YR, 100)
     hard = holo.hardening.Fixed_Time_2PL_SAM(sam, 3.0 * GYR, rchar=100.0 * PC, gamma_inner=-1.0, gamma_outer=2.5)
     fobs_orb_edges = fobs_gw_edges / 2.0
     fobs_orb_cents = 0.5 * (fobs_gw_edges[1:] + fobs_gw_edges[:-1]) / 2.0
     redz_final, dnum = sam_cyutils.dynamic_binary_number_at_fobs(fobs_orb_cents, sam, hard, holo.cosmo)
-    edges = [sam.mtot, sam.mrat, sam.redz, fobs_orb_edges]
-    number = sam_cyutils.integrate_differential_number_3dx1d(edges, dnum)
     keep = dict(redz_final_slice=_strided(redz_final, 17), dnum_slice=_strided(dnum, 17),
                 dnum_sum_f=dnum.sum(axis=(0, 1, 2)))
-    del dnum
-    h2fdf = gravwaves.char_strain_sq_from_bin_edges_redz(edges, redz_final)
-    del redz_final
-    w = number * h2fdf
+    nm, nq, nz, nf = dnum.shape
+    number_zf = np.zeros((nz - 1, nf))
+    hc2_zf = np.zeros((nz - 1, nf))
+    number_slice = np.zeros(((nm - 2) // 17 + 1, (nq - 2) // 17 + 1, (nz - 2) // 17 + 1, nf))
+    h2fdf_slice = np.zeros_like(number_slice)
+    slab = 17                       # a multiple of the slice stride, so slices align with slabs
+    for m0 in range(0, nm - 1, slab):
+        m1 = min(m0 + slab, nm - 1)
+        edges = [sam.mtot[m0:m1 + 1], sam.mrat, sam.redz, fobs_orb_edges]
+        num = sam_cyutils.integrate_differential_number_3dx1d(edges, dnum[m0:m1 + 1])
+        h2 = gravwaves.char_strain_sq_from_bin_edges_redz(edges, redz_final[m0:m1 + 1])
+        number_zf += num.sum(axis=(0, 1))
+        hc2_zf += (num * h2).sum(axis=(0, 1))
+        number_slice[m0 // 17] = num[0, ::17, ::17, :]
+        h2fdf_slice[m0 // 17] = h2[0, ::17, ::17, :]
     keep.update(mtot=sam.mtot, mrat=sam.mrat, redz=sam.redz, fobs_gw_edges=fobs_gw_edges, norm=hard._norm,
-                number_sum_f=number.sum(axis=(0, 1, 2)), mean_hc2_f=w.sum(axis=(0, 1, 2)),
-                mean_hc2_zf=w.sum(axis=(0, 1)), number_zf=number.sum(axis=(0, 1)),
-                number_slice=_strided(number, 17), h2fdf_slice=_strided(h2fdf, 17))
+                number_sum_f=number_zf.sum(axis=0), mean_hc2_f=hc2_zf.sum(axis=0), mean_hc2_zf=hc2_zf,
+                number_zf=number_zf, number_slice=number_slice, h2fdf_slice=h2fdf_slice)
     save("ref_cfg5.npz", **keep)
 
 
