@@ -115,16 +115,143 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def issue_roofline(instr, t_launch, clk, n_sm=152, schedulers=4):
-    """Warp-instruction issue rate of a launch against the GPU's peak (one instruction per clock per
-    SM sub-partition at the sampled maximum SM clock)."""
-    mhz = (clk or {}).get("sm_max_mhz") or 2070.0
-    if not instr or not t_launch:
-        return None
-    peak = n_sm * schedulers * mhz * 1e6
-    achieved = instr / t_launch
-    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
-            "instructions_per_launch": instr, "sm_mhz_for_peak": mhz}
+# ---- algorithmic cost of the realization stage, in thread instructions, declared from the
+# algorithms (not measured); the issue roofline is draws/s against (issue peak / ops per draw)
+OPS_UNIFORM = 10                 # Philox4x32-10: 10 rounds x (2 wide multiplies + 2 three-input XORs) / 4 words
+OPS_ACCUM = 5                    # count to float, times strain, Kahan add
+OPS_ALIAS = OPS_UNIFORM + 4 + OPS_ACCUM          # 0.1 <= lambda < 10: column, row word, compare, select
+OPS_TABLE = OPS_UNIFORM + 5 + OPS_ACCUM          # 10 <= lambda <= 47000: guide cell, flags, one compare
+OPS_TABLE_ENTRY = 4              # per table entry and realization group: recursion, to fixed point, prefix, store
+OPS_PTRS_ATTEMPT = 2 * OPS_UNIFORM + 25          # lambda > 47000: one transformed-rejection attempt
+PTRS_ATTEMPTS = 1.15             # expected attempts per draw (Hormann 1993)
+OPS_SPARSE_EVENT = 2 * OPS_UNIFORM + 6 + 5 + OPS_ACCUM   # lambda < 0.1, per event: gap, zero-truncated count
+OPS_STAGE = 10                   # per bin and frequency per realization group: load, classify
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except OSError:
+        return {}
+
+
+def realization_roofline(number, nreals, t_launch, n_sm, sm_mhz, waves):
+    """The realization kernel (k_bulk) against its issue roofline: every SM sub-partition issues one
+    warp instruction (32 thread instructions) per clock, and the workload needs ops_per_draw thread
+    instructions per (bin, frequency, realization) draw by the declared costs above, weighted by the
+    expectation histogram of this model.  The HBM view (algorithmic bytes over the launch time) is
+    kept as a sub-object; the kernel is not HBM-bound."""
+    import torch
+    lam = number.reshape(-1)
+    groups = -(-nreals // 1024)
+    sparse = (lam > 0) & (lam < 0.1)
+    alias = (lam >= 0.1) & (lam < 10.0)
+    table = (lam >= 10.0) & (lam <= 47000.0)
+    ptrs = lam > 47000.0
+    lt = lam[table]
+    sd = torch.sqrt(lt)
+    entries = float((torch.ceil(lt + 7.0 * sd + 6.0) - torch.clamp(torch.floor(lt - 7.0 * sd - 2.0), min=0.0)
+                     + 1.0).sum().item())
+    n_alias, n_table, n_ptrs = (int(m.sum().item()) for m in (alias, table, ptrs))
+    sparse_events = float(lam[sparse].sum().item())
+    ops = (nreals * (OPS_ALIAS * n_alias + OPS_TABLE * n_table + (OPS_PTRS_ATTEMPT * PTRS_ATTEMPTS + OPS_ACCUM) * n_ptrs)
+           + OPS_SPARSE_EVENT * nreals * sparse_events + OPS_TABLE_ENTRY * groups * entries
+           + OPS_STAGE * groups * lam.numel())
+    draws = lam.numel() * nreals
+    ops_per_draw = ops / draws
+    issue_peak = n_sm * 4 * 32 * sm_mhz * 1e6          # thread instructions / s
+    achieved = draws / t_launch
+    peak = issue_peak / ops_per_draw
+    # HBM view: every bin's expectation and the strain of the bins with a nonzero one (8 B each) per
+    # realization group, each realization's first bulk position, the per-chunk partial sums
+    nf = int(number.shape[-1])
+    nb = lam.numel() // nf
+    nchunk = max(1, -(-n_sm * 6 * waves // (nf * groups)))
+    n_pos = int((lam > 0).sum().item())
+    alg_bytes = (8 * nb * nf + 8 * n_pos) * groups + 4 * nf * nreals + 8 * nchunk * nf * nreals
+    hbm_peak = float(_peaks().get("hbm_gbs", 6800.0))
+    hbm = alg_bytes / t_launch / 1e9
+    n = lam.numel()
+    return {"kernel": "k_bulk", "bound": "issue", "unit": "draws/s", "achieved": achieved, "peak": peak,
+            "frac": achieved / peak, "launch_s": t_launch, "ops_per_draw": ops_per_draw,
+            "peak_issue_thread_instructions_per_s": issue_peak, "sm_mhz_for_peak": sm_mhz,
+            "draw_regimes": {"zero": int((lam <= 0).sum().item()) / n, "sparse_lt_0.1": int(sparse.sum().item()) / n,
+                             "alias_lt_10": n_alias / n, "table_le_47000": n_table / n, "ptrs_gt_47000": n_ptrs / n,
+                             "sparse_events_per_draw": sparse_events / n,
+                             "table_entries_per_bin_frequency": entries / n},
+            "traffic": 357620480,
+            "traffic_source": ("DRAM bytes read + written by one k_bulk launch of this workload, one ncu capture "
+                               "(profiles/k_bulk_91x81x101_f4_r1000.md)"),
+            "hbm": {"achieved": hbm, "peak": hbm_peak, "unit": "GB/s", "frac": hbm / hbm_peak,
+                    "algorithmic_bytes": alg_bytes},
+            "note": ("ops_per_draw from the costs declared in bench.py (OPS_*), weighted by this model's "
+                     "expectation histogram; the HBM floor of the launch is far below its time")}
+
+
+# per-element FP64 lane operations of the grid stages with a fixed per-element cost (additions and
+# multiplications are separate instructions: the parity mode is built without fused multiply-add)
+FP64_OPS_CELLS = {"fp64": 45, "fp32": 0}   # per (bin, frequency): 8-vertex sum and scale 11, midpoints 14,
+                                           # distance 12, (1+z)^(2/3) 2, strain product 6; FP32 mode: FP32
+                                           # arithmetic (FP64 only in sentinel-mixed midpoints)
+FP64_OPS_EVAL = {"fp64": 27, "fp32": 7}    # per bracketed element: redshift / distance interpolation 5, the
+                                           # rest of the residence time 22; FP32 mode: interpolation and the
+                                           # density products only
+
+
+def grid_stage_rooflines(H, C, fe, precision, n_sm, sm_mhz):
+    """One more model evaluation, stage by stage on one stream with CUDA events: the device time of
+    each grid stage, and for the dbn evaluation and number + strain stages (fixed per-element work)
+    their algorithmic FP64 and HBM fractions."""
+    import torch
+    from holodeck_gb300 import single_sources
+    from holodeck_gb300.sams import sam_cyutils
+    fp64_peak = 2.0 * n_sm * sm_mhz * 1e6   # FP64 lane operations / s (two per clock per SM)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+    ev[0].record()
+    sam, hard = make_model(H, C)
+    torch.cuda.current_stream().wait_event(hard._norm_ready)   # the normalisation runs on a side stream
+    ev[1].record()
+    dens, gmt_time, redz_prime = sam._static_density_launch()
+    ev[2].record()
+    sam._scatter_finish(dens, gmt_time, redz_prime)
+    ev[3].record()
+    mt, mr, rz = sam._edges_device()
+    fo_c = H.utils.midpoints(fe) / 2.0
+    rf, dn = sam_cyutils.dbn_2pwl_device(fo_c, hard, None, mt, mr, rz, gmt_time, phase=1)
+    ev[4].record()
+    rf, dn = sam_cyutils.dbn_2pwl_device(fo_c, hard, dens, mt, mr, rz, gmt_time, phase=2, out=(rf, dn),
+                                         precision=precision)
+    ev[5].record()
+    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf, precision=precision)
+    ev[6].record()
+    single_sources.sort_order_device(h2fdf)
+    ev[7].record()
+    torch.cuda.synchronize()
+    ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(7)]
+    nm, nq, nz = sam.shape
+    nf = int(number.shape[-1])
+    n_vf = nm * nq * nz * nf
+    n_bf = int(number.numel())
+    n_brk = int((rf >= 0).sum().item())
+    bytes_eval = 32 * n_brk + 8 * nm * nq * nz    # hint + time in, redshift + number out; the density
+    bytes_cells = 16 * n_vf + 16 * n_bf           # vertices in (each once from DRAM), number + strain out
+    hbm_peak = float(_peaks().get("hbm_gbs", 6800.0)) * 1e9
+
+    def fr(ops, nbytes, t_ms):
+        return {"ms": t_ms, "fp64_ops": ops, "fp64_frac": ops / (t_ms * 1e-3) / fp64_peak,
+                "hbm_bytes": nbytes, "hbm_frac": nbytes / (t_ms * 1e-3) / hbm_peak}
+
+    return {"precision": precision,
+            "stages_ms": {"model_build_and_hardening_norm": ms[0], "static_density": ms[1], "mbulge_scatter": ms[2],
+                          "dbn_step_walk": ms[3], "dbn_evaluation": ms[4], "number_and_strain": ms[5], "sort": ms[6]},
+            "dbn_evaluation": fr(FP64_OPS_EVAL[precision] * n_brk, bytes_eval, ms[4]),
+            "number_and_strain": fr(FP64_OPS_CELLS[precision] * n_bf, bytes_cells, ms[5]),
+            "fp64_peak_lane_ops_per_s": fp64_peak,
+            "note": ("stages run one after another here (gwb() overlaps the normalisation and the step walk with "
+                     "the density and scatter); FP64 ops per element declared in bench.py (FP64_OPS_*); the "
+                     "FP64-pipe utilisation of the iterative grid kernels is in profiles/")}
 
 
 def run_gpu(args):
@@ -218,11 +345,11 @@ def run_gpu(args):
     # ---- roofline of the realization kernel (CUDA events on the launching stream)
     sam, hard = make_model(H, C)
     fo_c = H.utils.midpoints(fe) / 2.0
-    rf, dn = sam._dbn_device(hard, fo_c)
-    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf)
+    rf, dn = sam._dbn_device(hard, fo_c, precision=args.precision)
+    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf, precision=args.precision)
+    del rf, dn
     order = single_sources.sort_order_device(h2fdf)
     from holodeck_gb300 import cyutils
-    nb = int(number.numel() // NFREQ)
     lib = N.load()
     N.check(lib.hgb_bulk_timing(1), "hgb_bulk_timing")
     times = []
@@ -233,32 +360,11 @@ def run_gpu(args):
         times.append(float(lib.hgb_bulk_last_ms()) / 1e3)
     N.check(lib.hgb_bulk_timing(0), "hgb_bulk_timing")
     t_real = sum(times) / len(times)
-    draws = nb * NFREQ * NREALS
-    # algorithmic bytes of one k_bulk launch, per realization group: every bin's expectation and the
-    # strain of the bins with a nonzero expectation (8 B each), each realization's first bulk
-    # position read, the per-chunk partials written
-    n_rgroups = -(-NREALS // 1024)
     n_sm = torch.cuda.get_device_properties(local).multi_processor_count
-    nchunk = max(1, -(-n_sm * 6 * lib.hgb_get_bulk_waves() // (NFREQ * n_rgroups)))
-    n_pos = int((number > 0).sum().item())
-    alg_bytes = (8 * nb * NFREQ + 8 * n_pos) * n_rgroups + 4 * NFREQ * NREALS + 8 * nchunk * NFREQ * NREALS
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
-            peaks = json.load(fh)
-    except OSError:
-        pass
-    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg_bytes / t_real / 1e9
-    traffic = None
-    instr = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
-            prof = json.load(fh)
-            traffic = prof.get("k_bulk_bytes_per_launch")
-            instr = prof.get("k_bulk_warp_instructions_per_launch")
-    except (OSError, ValueError):
-        pass
+    sm_mhz = (clk or {}).get("sm_max_mhz") or 2070.0
+    roofline = realization_roofline(number, NREALS, t_real, n_sm, sm_mhz, lib.hgb_get_bulk_waves())
+    del number, h2fdf, order
+    grid_stages = grid_stage_rooflines(H, C, fe, args.precision, n_sm, sm_mhz)
 
     batched = run_batched(args, rank, world) if args.batched_samples > 0 else None
     highres = None
@@ -271,27 +377,26 @@ def run_gpu(args):
     cpu = hc_error = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, keep = cpu_baseline_sample(args)
-        hc_error = hc_error_vs_oracle(keep)
+        hc_error = hc_error_vs_reference(keep, args.precision)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 grids / f32+int32 realizations",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": ("f64 grids / f32+int32 realizations" if args.precision == "fp64" else
+                      "f32 grid arithmetic (f64 density, hardening integral, age->redshift inversion) / "
+                      "f32+int32 realizations"),
             "data": "synthetic (analytic model parameters; no dataset)",
             "config": {"workload": CONFIG_NAME, "grid": list(SHAPE), "nfreqs": NFREQ, "nreals": NREALS,
-                       "nloudest": NLOUD, "rng": "philox4x32-10", "l2": "flushed (256 MB write) before every step",
+                       "nloudest": NLOUD, "precision": args.precision, "rng": "philox4x32-10",
+                       "l2": "flushed (256 MB write) before every step",
                        "parallelism": f"replicas x{world}",
                        "note": "scatter geometry plan cached per grid; every other stage recomputed each step"},
             "e2e": {"value": world * NREALS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"kernel": "k_bulk", "bound": "hbm", "achieved": achieved, "peak": hbm_peak,
-                         "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                         "launch_s": t_real, "draws_per_s": draws / t_real,
-                         "issue": issue_roofline(instr, t_real, clk),
-                         "note": ("issue-bound sampler: the HBM fraction is shown for the contract; the "
-                                  "issue object is the bound that applies (warp instructions per launch "
-                                  "from ncu, see profiles/)")},
+            "roofline": roofline,
+            "grid_stages": grid_stages,
             "clocks": clk,
             "cpu_baseline": cpu,
             "hc_error": hc_error,
@@ -424,75 +529,46 @@ def run_emulator(args):
 
 
 # ------------------------------------------------------------------------------------------------
-# CPU restatement (oracle): bounded sample, extrapolated to the full workload
+# The reference on the host cores: its compiled Cython kernels (oracle/ref_build.py) driven by the
+# oracle's restatement of its Python glue (oracle/ref_stub.py), on bounded samples
 # ------------------------------------------------------------------------------------------------
 
-SAMPLE_Z = 11
-SAMPLE_R = 3
+SAMPLE_Z = 11   # the GPU line's single-core sample: the 91 x 81 x 11 grid
+SAMPLE_R = 3    # realizations drawn per sample (the rest is extrapolated linearly in R)
+REF_SAMPLE_R = 3
 
 
-def _oracle_sample(seed, nreals, keep=None):
-    """Times the oracle path on the sample grid (91 x 81 x 11): stage seconds.  With ``keep`` (a
-    dict) it also receives the sample's edges, frequency edges, grids and loudest-first order."""
-    from oracle import sam_oracle as O
-    from holodeck_gb300 import constants as C
-    shape = (SHAPE[0], SHAPE[1], SAMPLE_Z)
-    mtot, mrat, redz = O.grid_edges(shape)
-    p = O.default_params(scatter_dex=0.28)
-    t = {}
-    t0 = time.perf_counter()
-    parts = O.static_binary_density(mtot, mrat, redz, p, return_parts=True)
-    t["density"] = time.perf_counter() - t0
-    mt, mr = np.meshgrid(mtot, mrat, indexing="ij")
-    t0 = time.perf_counter()
-    norm = 10.0 ** O.find_2pwl_hardening_norm(3.0 * C.GYR, mt.ravel(), mr.ravel(), 1.0e3 * C.PC, 100.0 * C.PC,
-                                              -1.0, 2.5, 300).reshape(mt.shape)
-    t["norm"] = time.perf_counter() - t0
-    _, fe = O.pta_freqs(16.0 * C.YR, NFREQ)
-    fo_c = O.midpoints(fe) / 2.0
-    t0 = time.perf_counter()
-    rf, dn = O.dbn_2pwl(fo_c, 1.0e3 * C.PC, 300, norm, 100.0 * C.PC, -1.0, 2.5, parts["density"], mtot, mrat, redz,
-                        parts["gmt_time"])
-    t["dbn"] = time.perf_counter() - t0
-    edges = [mtot, mrat, redz, fe / 2.0]
-    t0 = time.perf_counter()
-    number = O.integrate_differential_number_3dx1d(edges, dn)
-    h2fdf = O.char_strain_sq_from_bin_edges_redz(edges, rf)
-    order = O.sort_order(h2fdf)
-    t["integrate_strain"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.loudest_hc_from_sorted(number, h2fdf, nreals, NLOUD, order, seed=seed)
-    t["realize"] = time.perf_counter() - t0
-    if keep is not None:
-        keep.update(edges=[mtot, mrat, redz], fobs_gw_edges=fe, number=number, h2fdf=h2fdf, order=order,
-                    redz_final=rf)
-    return t
-
-
-def _extrapolate(t, nreals_sampled):
-    """Full-workload seconds per model: the Z-sliced stages scale with the redshift bins, the
-    hardening normalisation is Z-independent, realizations scale with bins and count."""
-    zscale = (SHAPE[2] - 1) / (SAMPLE_Z - 1)
-    grid = zscale * (t["density"] + t["dbn"] + t["integrate_strain"]) + t["norm"]
-    per_real = zscale * t["realize"] / nreals_sampled
+def _ref_per_model(t, nreals_sampled, zscale=1.0):
+    """Seconds of one full model (the 91 x 81 x 101 grid, NREALS realizations) from the stage
+    seconds of a sample: the redshift-sliced stages scale with the redshift bins (zscale), the
+    hardening normalisation does not, realizations scale with bins and count."""
+    grid = zscale * sum(v for k, v in t.items() if k not in ("hardening_norm", "realizations"))
+    grid += t["hardening_norm"]
+    per_real = zscale * t["realizations"] / nreals_sampled
     return grid + NREALS * per_real, grid, per_real
 
 
 def cpu_baseline_sample(args):
+    """The reference's path on one host core on the 91 x 81 x 11 sample (about 10 s), extrapolated
+    to the bench workload; also keeps the sample's FP64 grids for the hc error of the GPU path."""
+    from oracle import ref_stub
     keep = {}
-    t = _oracle_sample(seed=7, nreals=SAMPLE_R, keep=keep)
-    total, grid, per_real = _extrapolate(t, SAMPLE_R)
-    return {"value": NREALS / total, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": (f"oracle on grid 91x81x{SAMPLE_Z} with {SAMPLE_R} realizations, extrapolated linearly in "
-                       f"redshift bins and realizations: grid stages {grid:.1f} s + {per_real:.2f} s/realization "
+    t = ref_stub.reference_gwb_stages((SHAPE[0], SHAPE[1], SAMPLE_Z), NFREQ, SAMPLE_R, NLOUD, seed=7, keep=keep)
+    total, grid, per_real = _ref_per_model(t, SAMPLE_R, zscale=(SHAPE[2] - 1) / (SAMPLE_Z - 1))
+    return {"value": NREALS / total, "unit": UNIT, "cores": 1, "kind": "reference",
+            "sample": (f"the reference's compiled Cython kernels (cyutils.pyx, sam_cyutils.pyx built from its "
+                       f"sources) with the oracle's restatement of its Python glue, one process, on grid "
+                       f"91x81x{SAMPLE_Z} with {SAMPLE_R} realizations, extrapolated linearly in redshift bins and "
+                       f"realizations: grid stages {grid:.1f} s + {per_real:.2f} s/realization "
                        f"({', '.join(f'{k} {v:.2f}s' for k, v in t.items())})")}, keep
 
 
-def hc_error_vs_oracle(keep, nreals=8):
-    """The GPU path's strain against the FP64 oracle on the CPU baseline's sample model (the bench
-    model on a 91 x 81 x 11 grid, 40 frequencies): the oracle's grids and numpy-PCG64 Poisson counts
-    replayed through the public gwb(); max relative error of hc_ss and hc_bg, and of the number and
-    strain grids."""
+def hc_error_vs_reference(keep, precision, nreals=8):
+    """The GPU path (in ``precision``) against the reference's FP64 kernels on the CPU baseline's
+    sample model (the bench model on the 91 x 81 x 11 grid, 40 frequencies): numpy-PCG64 Poisson
+    counts drawn from the reference's expectations and replayed in its visiting order through the
+    public gwb(); relative errors of hc_ss and hc_bg (max, and per frequency), of the expected hc^2
+    sum_b number h2fdf per frequency, and of the number and strain grids."""
     import holodeck_gb300 as H
     from holodeck_gb300 import constants as C
     from oracle import sam_oracle as O
@@ -501,9 +577,14 @@ def hc_error_vs_oracle(keep, nreals=8):
     counts = O.replay_counts(keep["number"], keep["order"], nreals, 11)
     ss_o, bg_o = O.ss_gws_redz(keep["edges"] + [fe / 2.0], keep["redz_final"], keep["number"], nreals, NLOUD,
                                counts=counts)
-    ss, bg = sam.gwb(fe, hard=hard, realize=nreals, loudest=NLOUD, replay=counts, order=keep["order"])
-    rf, dn = sam._dbn_device(hard, O.midpoints(fe) / 2.0)
-    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf)
+    ss, bg = sam.gwb(fe, hard=hard, realize=nreals, loudest=NLOUD, replay=counts, order=keep["order"],
+                     precision=precision)
+    rf, dn = sam._dbn_device(hard, O.midpoints(fe) / 2.0, precision=precision)
+    number, h2fdf = sam._number_and_strain(fe / 2.0, dn, rf, precision=precision)
+    number, h2fdf = number.cpu().numpy(), h2fdf.cpu().numpy()
+    nf = number.shape[-1]
+    mean_o = (keep["number"] * keep["h2fdf"]).reshape(-1, nf).sum(0)
+    mean_g = (number * h2fdf).reshape(-1, nf).sum(0)
 
     def rel(a, b):
         a, b = np.asarray(a), np.asarray(b)
@@ -511,52 +592,69 @@ def hc_error_vs_oracle(keep, nreals=8):
         m = scale > 0
         return float((np.abs(a - b)[m] / scale[m]).max()) if m.any() else 0.0
 
+    def sig_rel(a, b, floor=1e-25):   # over values that can reach the strain (FP32 flushes below FLT_MIN)
+        a, b = np.asarray(a), np.asarray(b)
+        m = np.abs(b) > floor * np.abs(b).max()
+        return float((np.abs(a[m] - b[m]) / np.abs(b[m])).max())
+
     return {"case": (f"bench model on the 91x81x{SAMPLE_Z} grid, {NFREQ} frequencies, {nreals} realizations replayed "
-                     "from numpy PCG64 Poisson draws, against the FP64 CPU oracle"),
+                     f"from numpy PCG64 Poisson draws, GPU path in {precision} against the reference's FP64 kernels"),
+            "precision": precision,
             "hc_ss_max_rel": rel(ss, ss_o), "hc_bg_max_rel": rel(bg, bg_o),
-            "hc_bg_max_rel_per_freq": [rel(bg[f], bg_o[f]) for f in range(bg.shape[0])],
-            "number_max_rel": rel(number.cpu().numpy(), keep["number"]),
-            "h2fdf_max_rel": rel(h2fdf.cpu().numpy(), keep["h2fdf"])}
+            "hc_ss_max_rel_per_freq": [rel(ss[f], ss_o[f]) for f in range(nf)],
+            "hc_bg_max_rel_per_freq": [rel(bg[f], bg_o[f]) for f in range(nf)],
+            "mean_hc2_rel_per_freq": [float(abs(mean_g[f] / mean_o[f] - 1.0)) for f in range(nf)],
+            "number_max_rel": sig_rel(number, keep["number"]), "h2fdf_max_rel": sig_rel(h2fdf, keep["h2fdf"])}
 
 
-def _worker(args):
-    seed, nreals = args
-    return _oracle_sample(seed, nreals)
+def _ref_worker(seed):
+    from oracle import ref_stub
+    return ref_stub.reference_gwb_stages(SHAPE, NFREQ, REF_SAMPLE_R, NLOUD, seed=seed)
 
 
 def run_reference(args):
-    """Reference arm: the CPU restatement on all host cores (one sample model per worker process)."""
+    """Reference arm: the reference's path (its compiled Cython kernels with the oracle's restatement of
+    its Python glue) on every host core, each worker one evaluation of the full 91 x 81 x 101 grid with
+    REF_SAMPLE_R realizations, extrapolated linearly in the realization count.  The reference is
+    serial, so the cores run independent model evaluations, as its MPI library driver does."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import multiprocessing as mp
+    from oracle import ref_build
+    if not ref_build.generated():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's Cython kernels were not generated "
+                          "(oracle/ref_build.py generate needs the reference sources and Cython)"}))
+        return
+    ref_build.compile()
     ncores = os.cpu_count() or 1
+    nsamples = args.warmup + args.steps
+    nproc = min(ncores, nsamples)
     ctx = mp.get_context("spawn")
-    results = []
-    with ctx.Pool(ncores) as pool:
-        for i in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            res = pool.map(_worker, [(1000 * i + k, SAMPLE_R) for k in range(ncores)])
-            wall = time.perf_counter() - t0
-            if i >= args.warmup:
-                results.append((wall, res))
-    # each worker ran the same sample model; the pool finishes ncores samples per wall time
-    per_model = []
-    for wall, res in results:
-        cpu_total = sum(_extrapolate(t, SAMPLE_R)[0] for t in res) / len(res)
-        cpu_sample = sum(sum(t.values()) for t in res) / len(res)
-        per_model.append(cpu_total * (wall / cpu_sample) / ncores)   # wall-clock seconds per full model
-    sec = statistics.median(per_model)
-    value = NREALS / sec
+    t_wall = time.perf_counter()
+    with ctx.Pool(nproc) as pool:
+        res = pool.map(_ref_worker, [1000 + k for k in range(nsamples)], chunksize=1)
+    t_wall = time.perf_counter() - t_wall
+    timed = res[args.warmup:]
+    per_model = [_ref_per_model(t, REF_SAMPLE_R)[0] for t in timed]
+    sec = statistics.median(per_model)   # one core's seconds per full model, measured with every core busy
+    value = nproc * NREALS / sec
+    stages = {k: round(statistics.median(t[k] for t in timed), 3) for k in timed[0]}
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_wall * 1e3 / nsamples,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": CONFIG_NAME, "grid": list(SHAPE), "nfreqs": NFREQ, "nreals": NREALS,
                        "nloudest": NLOUD},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": ncores, "kind": "port",
-                             "sample": (f"{ncores} processes, each the oracle on grid 91x81x{SAMPLE_Z} with "
-                                        f"{SAMPLE_R} realizations per step, extrapolated linearly to the full "
-                                        "workload")},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nproc, "kind": "reference",
+                             "sample": (f"{nproc} processes, each step one evaluation of the full 91x81x101 grid "
+                                        f"through the reference's compiled Cython kernels (cyutils.pyx, "
+                                        f"sam_cyutils.pyx, built from its sources) and the oracle's restatement of "
+                                        f"its Python glue, with {REF_SAMPLE_R} realizations, extrapolated linearly "
+                                        f"in the realization count; {nsamples} evaluations in {t_wall:.0f} s"),
+                             "stage_seconds_median": stages,
+                             "seconds_per_model_one_core": sec,
+                             "note": ("ms_per_step is the wall time per sampled evaluation with every core busy; "
+                                      "value extrapolates each sample to the workload's 1000 realizations")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
