@@ -511,7 +511,8 @@ __global__ void k_dbn_2pwl_eval_f32(CyConst cc, Dbn2plArgs a, const double *__re
     __shared__ int s_e0;
     if (threadIdx.x == 0) {
         const double mt = mtot[ii], mr = mrat[jj], norm = hard_norm[cell];
-        const double gc = fabs(cc.c_dadt) * pow(mt, 3.0) * mr / pow(1.0 + mr, 2.0) / pow(a.rchar, 3.0);
+        const double opq = 1.0 + mr, rc = a.rchar;   // products in place of powers: one thread, the block waits
+        const double gc = fabs(cc.c_dadt) * (mt * mt * mt) * mr / (opq * opq) / (rc * rc * rc);
         int ea = -100000, eg = -100000;
         if (norm > 0.0) frexp(norm, &ea);
         if (gc > 0.0) frexp(gc, &eg);
@@ -519,7 +520,7 @@ __global__ void k_dbn_2pwl_eval_f32(CyConst cc, Dbn2plArgs a, const double *__re
         s_e0 = e0;
         s_as = (float)ldexp(norm, -e0);   // in [0.5, 1) or flushed to 0 when negligible
         s_gs = (float)ldexp(gc, -e0);
-        s_k13 = (float)(cc.ksepa * pow(mt, 1.0 / 3.0));
+        s_k13 = (float)(cc.ksepa * cbrt(mt));
         s_rchar_inv = (float)(1.0 / a.rchar);
     }
     __syncthreads();

@@ -189,11 +189,15 @@ __global__ void k_cells_f32(BinGeom g, StrainArgs32 s, double amp_scale, const d
     for (int z = threadIdx.x; z < g.nz - 1; z += blockDim.x)
         s_vol[z] = hgb::f64_to_f32_rz(dmdq * (redz[z + 1] - redz[z])) * 0.125f;
     if (threadIdx.x == 0) {
+        // K mc (2 mc)^(2/3) = K 2^(2/3) mc^(5/3) with mc^(5/3) = mt^(5/3) mr / (1 + mr)^2 for the chirp
+        // mass mc = mt mr^(3/5) / (1 + mr)^(6/5): one cube root instead of three powers on the one
+        // thread the block waits for
         const double mt = 0.5 * (mtot[m + 1] + mtot[m]);
         const double mr = 0.5 * (mrat[q + 1] + mrat[q]);
-        const double mc = mt * pow(mr, 3.0 / 5.0) / pow(1.0 + mr, 6.0 / 5.0);
+        const double c = cbrt(mt), opq = 1.0 + mr;
+        const double mc53 = mt * (c * c) * mr / (opq * opq);
         int ka;
-        const double mant = 2.0 * frexp(amp_scale * mc * pow(2.0 * mc, 2.0 / 3.0), &ka);
+        const double mant = 2.0 * frexp(amp_scale * 1.5874010519681994 * mc53, &ka);   // 2^(2/3)
         s_amp_mq = (float)mant;
         s_ka = ka - 1;
     }
