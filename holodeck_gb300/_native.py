@@ -195,7 +195,7 @@ def check(rc, what):
 KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_2pwl_phase_f32": 1, "hgb_dbn_gw": 1,
-    "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_number_and_strain_f32": 1, "hgb_argsort_f0_desc": 11,
+    "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_number_and_strain_f32": 1, "hgb_argsort_f0_desc": 25, "hgb_argsort_f0_desc_static": 25,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
     "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1,
 }

@@ -22,6 +22,12 @@ namespace hgb {
 void set_cuda_error(cudaError_t err);
 int check_launch();
 
+// Loudest-first argsort at the first frequency (hgb_sort.cu): scratch bytes for n_bins, and the sort
+// itself with the caller's scratch (at least argsort_f0_scratch_bytes(n_bins), 256-byte aligned).
+size_t argsort_f0_scratch_bytes(long n_bins);
+int argsort_f0_desc_into(const double *h2fdf, long n_bins, int n_freq, int32_t *order, void *scratch,
+                         cudaStream_t st);
+
 __device__ __forceinline__ void flag(int *d_status, int bits) {
     if (d_status) atomicOr(d_status, bits);
 }

@@ -275,7 +275,9 @@ int hgb_number_and_strain_f32(const double *mtot, const double *log10_mtot, int 
  * whose order among equal keys depends on the sort's partitioning.  Bins whose keys tie can
  * therefore be visited in another order than the reference visits them; callers that must
  * reproduce the reference's visiting order exactly pass its order to the realization entry
- * points instead. */
+ * points instead.  -0.0 ties with +0.0 and NaN keys come last, as in numpy's argsort of the
+ * negated keys.  The sort is this library's own stable radix sort (8 passes of 8 bits, 25 kernel
+ * launches); workspace: hgb_sort_workspace_bytes(n_bins), about 20 bytes per bin. */
 size_t hgb_sort_workspace_bytes(long n_bins);
 int hgb_argsort_f0_desc(const double *h2fdf, long n_bins, int n_freq, int32_t *order,
                         void *workspace, size_t workspace_bytes, void *stream);

@@ -129,6 +129,29 @@ def test_sort_order(built_lib):
     assert np.array_equal(order[~tied], g["order"][~tied])
 
 
+@pytest.mark.parametrize("nb", [1, 2, 255, 2048, 2049, 100003, 1 << 20])
+def test_sort_order_edge_values(built_lib, nb):
+    """The radix argsort equals numpy's stable argsort of the negated first-frequency keys: ties in
+    ascending bin order, -0.0 tied with +0.0, NaNs last; ragged tile ends and a strided frequency axis."""
+    import torch
+    from holodeck_gb300 import single_sources
+    rng = np.random.default_rng(nb)
+    nf = 3
+    h = rng.lognormal(-40.0, 3.0, size=(nb, nf))
+    pick = rng.random(nb)
+    h[pick < 0.2, 0] = 0.0
+    h[(pick >= 0.2) & (pick < 0.25), 0] = -0.0
+    h[(pick >= 0.25) & (pick < 0.3), 0] = 1.5e-30   # a tie run
+    h[(pick >= 0.3) & (pick < 0.31), 0] = np.nan
+    h[(pick >= 0.31) & (pick < 0.32), 0] = -rng.random(int(((pick >= 0.31) & (pick < 0.32)).sum()))
+    h[(pick >= 0.32) & (pick < 0.33), 0] = np.inf
+    h[(pick >= 0.33) & (pick < 0.34), 0] = 5e-324
+    key = h[:, 0]
+    want = np.argsort(-key, kind="stable")
+    got = single_sources.sort_order_device(torch.as_tensor(h, device="cuda")).cpu().numpy()
+    assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("name", ["ref_small_2pwl_noscatter.npz", "ref_small_2pwl_scatter.npz",
                                   "ref_small_gw_noscatter.npz"])
 def test_loudest_replay_bit_exact(built_lib, name):

@@ -44,10 +44,13 @@ def test_static_sort_matches_workspace_entry_point(built_lib):
     # a large case with many exact ties and zeros (stable order among equal keys)
     big = rng.choice(np.array([0.0, 1e-30, 2e-30, 3e-28]), size=(700_000, 3)) * rng.integers(1, 4, size=(700_000, 3))
     big = torch.as_tensor(big, device="cuda")
-    for h in (golden, big, golden):   # consecutive calls, sizes changing between them
+    # the capacity itself: 2^20 bins
+    full = torch.as_tensor(rng.lognormal(-40.0, 3.0, size=(1 << 20, 2)), device="cuda")
+    for h in (golden, big, full, golden):   # consecutive calls, sizes changing between them
         ref = single_sources.sort_order_device(h).cpu().numpy()
         first = _static_order(h).cpu().numpy()
         second = _static_order(h).cpu().numpy()
         assert np.array_equal(first, ref)
         assert np.array_equal(second, ref)
+        assert np.array_equal(first, np.argsort(-h[:, 0].cpu().numpy(), kind="stable"))
     torch.cuda.synchronize()
