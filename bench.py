@@ -428,7 +428,7 @@ def run_batched(args, rank=0, world=1):
     shapes, nreals = batch.random_shapes(n, seed=0)
     stats = {}
     out = batch.run_library(space, shapes, nreals, nfreqs=NFREQ, nloudest=NLOUD, seed=1,
-                            indices=batch.shard_indices(n, rank, world), stats=stats)
+                            indices=batch.shard_indices(n, rank, world), stats=stats, precision=args.precision)
     job = batch.reduce_stats(stats)                       # max wall time, summed work over the replicas
     wall, reals, draws = job["seconds"], job["realizations"], job["draws"]
     d2h = sum(sum(v.nbytes for k, v in r.items() if isinstance(v, np.ndarray)) for r in out if r is not None)
@@ -437,7 +437,7 @@ def run_batched(args, rank=0, world=1):
     ones = [v for k, v in table.items() if k.split(",")[0] == "1"]
     one = max(ones) if ones else None
     best = table.get(f"{stats['workers']},{stats['waves']}")
-    return {"workload": BATCH_CONFIG, "samples": n, "failed": job["failed"], "seconds": wall,
+    return {"workload": BATCH_CONFIG, "precision": args.precision, "samples": n, "failed": job["failed"], "seconds": wall,
             "value": reals / wall, "unit": UNIT, "samples_per_s": n / wall, "draws_per_s": draws / wall,
             "realizations": int(reals), "schedule": {"workers": stats["workers"], "waves": stats["waves"]},
             "autotune_draws_per_s": table,

@@ -13,7 +13,7 @@
 //   3. k_back_dot: the Gaussian redistribution W^T (W^T G) as the reference computes it (see
 //      hgb_add_scatter_to_masses) followed by the bilinear interpolation back to the points, fused
 //      into one dot product per (point, slice) with the plan's per-point row of (W W).
-// FP64 throughout; built with -fmad=false.
+// FP64 throughout; built with -fmad=false (k_gradients_lv fuses its multiply-adds explicitly).
 #include <math.h>
 
 #include "hgb_common.cuh"
@@ -92,8 +92,14 @@ __global__ void k_gradients(hgb_scatter_plan P, const double *__restrict__ dens,
 //     double-buffered in shared memory) while warps 0 and 1 update the current ones.
 // The static data of the next level (each warp's first LV_REG edges of its point, the rows of the
 // inverse normal matrix that warps 0 and 1 use) is loaded into registers while the current level
-// computes.  Per point the terms and the test are those of k_gradients; only the grouping of the
-// neighbour sum differs (four interleaved partial sums).
+// computes.  Per point the terms and the test are those of k_gradients, with two differences of
+// rounding: the neighbour sum is grouped as four interleaved partial sums, and the multiply-adds are
+// fused (explicit __fma_rn, the file being built with -fmad=false).  An edge term
+//   c = 6 (f_j - f_i) - 2 (g_jx w0 + g_jy w1),  sx += c w2,  sy += c w3
+// takes 6 FP64 instructions instead of 11: the plan stores -2 w0 and -2 w1 (an exact scaling), so
+//   t = fma(g_jy, -2 w1, g_jx (-2 w0)),  c = fma(6, f_j - f_i, t),  sx = fma(c, w2, sx),  sy = fma(c, w3, sy),
+// and the 2x2 solve takes 2 instead of 3.  The FP64 pipe bounds this kernel, so the instruction
+// count is its time; each fused operation skips one rounding (an ulp of the term).
 constexpr int LV_WARPS = 4;
 constexpr int LV_REG = 3;   // edges o, o+4, o+8 per warp: interior points have 6 neighbours
 
@@ -186,10 +192,10 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                         for (int k = 0; k < LV_REG; k++) {
                             if (e < e1) {
                                 const int j = cur.idx[k];
-                                const double cc = 6.0 * (f[j] - fi) -
-                                                  2.0 * (g[2 * j] * cur.w01[k].x + g[2 * j + 1] * cur.w01[k].y);
-                                sx += cc * cur.w23[k].x;
-                                sy += cc * cur.w23[k].y;
+                                const double tt = __fma_rn(g[2 * j + 1], cur.w01[k].y, g[2 * j] * cur.w01[k].x);
+                                const double cc = __fma_rn(6.0, f[j] - fi, tt);
+                                sx = __fma_rn(cc, cur.w23[k].x, sx);
+                                sy = __fma_rn(cc, cur.w23[k].y, sy);
                             }
                             e += LV_WARPS;
                         }
@@ -198,9 +204,10 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                         const int j = __ldg(P.lv_nbr + e);
                         const double2 w01 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e));
                         const double2 w23 = __ldg((const double2 *)(P.lv_nbr_w + 4 * (long)e + 2));
-                        const double cc = 6.0 * (f[j] - fi) - 2.0 * (g[2 * j] * w01.x + g[2 * j + 1] * w01.y);
-                        sx += cc * w23.x;
-                        sy += cc * w23.y;
+                        const double tt = __fma_rn(g[2 * j + 1], w01.y, g[2 * j] * w01.x);
+                        const double cc = __fma_rn(6.0, f[j] - fi, tt);
+                        sx = __fma_rn(cc, w23.x, sx);
+                        sy = __fma_rn(cc, w23.y, sy);
                     }
                 }
                 psx[warp][lane] = sx;
@@ -213,7 +220,7 @@ __global__ void __launch_bounds__(32 * LV_WARPS, 1) k_gradients_lv(hgb_scatter_p
                         const double tx = ((psx[0][lane] + psx[1][lane]) + psx[2][lane]) + psx[3][lane];
                         const double ty = ((psy[0][lane] + psy[1][lane]) + psy[2][lane]) + psy[3][lane];
                         const double2 q = pre ? cur.q : __ldg((const double2 *)(P.lv_qinv + 4 * (long)p + 2 * warp));
-                        const double nv = q.x * tx + q.y * ty;
+                        const double nv = __fma_rn(q.y, ty, q.x * tx);
                         dv = fabs(nv - g[2 * p + warp]);
                         av = fabs(nv);
                         g[2 * p + warp] = nv;

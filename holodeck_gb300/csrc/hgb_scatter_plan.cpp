@@ -433,7 +433,8 @@ int hgb_scatter_plan_build(const double *mtot, int n_mtot, const double *mrat, i
             plan->lv_nbr_ptr[p] = e;
             for (int q = plan->nbr_ptr[i]; q < plan->nbr_ptr[i + 1]; q++, e++) {
                 plan->lv_nbr[e] = pos_of[plan->nbr_idx[q]];
-                for (int c = 0; c < 4; c++) plan->lv_nbr_w[4 * e + c] = plan->nbr_w[4 * q + c];
+                // -2 w0, -2 w1, w2, w3: the level-order solve folds the factor -2 into its weights
+                for (int c = 0; c < 4; c++) plan->lv_nbr_w[4 * e + c] = (c < 2 ? -2.0 : 1.0) * plan->nbr_w[4 * q + c];
             }
             for (int c = 0; c < 4; c++) plan->lv_qinv[4 * p + c] = plan->vtx_qinv[4 * i + c];
         }

@@ -149,7 +149,7 @@ typedef struct {    /* host arrays, sized by hgb_scatter_plan_bounds */
     /* the neighbourhoods again, indexed by level-order position p (point level_vtx[p]) */
     int32_t *lv_nbr_ptr; /* [n_pts+1] */
     int32_t *lv_nbr;    /* [n_nbr] neighbour positions, in the order of nbr_idx */
-    double *lv_nbr_w;   /* [n_nbr][4] */
+    double *lv_nbr_w;   /* [n_nbr][4]: -2 w0, -2 w1, w2, w3 of nbr_w, in level order */
     double *lv_qinv;    /* [n_pts][4] */
 } hgb_scatter_host_plan;
 
