@@ -131,6 +131,8 @@ class DeviceCosmology:
         s.dcg_val = N.ptr(self.dcg_val)
         s.dcg_der = N.ptr(self.dcg_der)
         self.struct = s
+        # cached and used from every stream: the uploads are complete before the cache hands it out
+        t.cuda.current_stream(device(dev)).synchronize()
 
     @property
     def ref(self):

@@ -169,6 +169,12 @@ __host__ __device__ __forceinline__ long ceil_div(long a, long b) { return (a + 
 // Multiprocessor count of the current device (queried once per device, 152 on a GB300).
 int sm_count();
 
+// Make `func` launchable with `bytes` of dynamic shared memory on the current device.  The cap
+// (cudaFuncAttributeMaxDynamicSharedMemorySize) is per function and shared by every host thread, so
+// it is only ever raised, under a lock: a thread that sets a smaller cap between another thread's
+// set and launch would make that launch fail with cudaErrorLaunchOutOfResources.
+int ensure_dyn_smem(const void *func, size_t bytes);
+
 }  // namespace hgb
 
 #define HGB_CHECK_ARG(cond)                        \

@@ -815,24 +815,13 @@ int hgb_find_2pwl_hardening_norm(double target_time, const double *mtot, const d
     if (wpb > 4) wpb = 4;
     if (wpb < 1) wpb = 1;
     size_t smem = per_warp * wpb;
-    if (smem > 48 * 1024) {
-        cudaError_t err = cudaFuncSetAttribute(k_hardening_norm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
-        if (err != cudaSuccess) {
-            hgb::set_cuda_error(err);
-            return HGB_ERR_CUDA;
-        }
-    }
+    int rc = hgb::ensure_dyn_smem((const void *)k_hardening_norm, smem);
+    if (rc) return rc;
     NormArgs a{target_time, log10(sepa_init), rchar, gamma_inner, gamma_outer, nsteps,
                pow_plan(-gamma_outer + gamma_inner), pow_plan(gamma_inner - 1.0)};
     if (nsteps + 1 <= 32 * NB_NODES) {
         const size_t bsmem = norm_blk_smem(nsteps);
-        cudaError_t err = cudaFuncSetAttribute(k_hardening_norm_blk, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)bsmem);
-        if (err != cudaSuccess) {
-            hgb::set_cuda_error(err);
-            return HGB_ERR_CUDA;
-        }
+        if ((rc = hgb::ensure_dyn_smem((const void *)k_hardening_norm_blk, bsmem))) return rc;
         k_hardening_norm_blk<<<(unsigned)hgb::ceil_div(n, NB_CELLS), NB_CELLS * 32, bsmem, (cudaStream_t)stream>>>(
             hgb::cy_const(), a, mtot, mrat, n, norm_log10, norm, d_status);
         return hgb::check_launch();
@@ -863,14 +852,8 @@ int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, doub
         size_t smem = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
                                         2 * (size_t)num_steps);
         HGB_CHECK_ARG(smem <= 200 * 1024);
-        if (smem > 48 * 1024) {
-            cudaError_t err = cudaFuncSetAttribute(k_dbn_2pwl, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)smem);
-            if (err != cudaSuccess) {
-                hgb::set_cuda_error(err);
-                return HGB_ERR_CUDA;
-            }
-        }
+        int src = hgb::ensure_dyn_smem((const void *)k_dbn_2pwl, smem);
+        if (src) return src;
         int threads = ((n_redz + 31) / 32) * 32;
         if (threads > 256) threads = 256;
         k_dbn_2pwl<<<blocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden,

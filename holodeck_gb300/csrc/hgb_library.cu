@@ -3,6 +3,9 @@
 #include <stdio.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "hgb_common.cuh"
 
@@ -42,6 +45,28 @@ int sm_count() {
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
     cache[dev].store(n, std::memory_order_relaxed);
     return n;
+}
+
+int ensure_dyn_smem(const void *func, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> raised;   // (function, device) -> cap set
+    if (bytes <= 48 * 1024) return HGB_OK;   // within the default cap
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) {
+        set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cap = raised[std::make_pair(func, dev)];
+    if (bytes <= cap) return HGB_OK;
+    err = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err != cudaSuccess) {
+        set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    cap = bytes;
+    return HGB_OK;
 }
 
 CyConst cy_const() {

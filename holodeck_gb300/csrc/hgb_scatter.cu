@@ -386,7 +386,8 @@ int hgb_add_scatter_to_masses(const hgb_scatter_plan *plan, double *dens, int n_
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (P.lv_nbr_ptr && P.lv_nbr && P.lv_nbr_w && P.lv_qinv && lv_smem + 8192 <= (size_t)smem_optin) {
-        cudaFuncSetAttribute(k_gradients_lv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lv_smem);
+        const int rc = hgb::ensure_dyn_smem((const void *)k_gradients_lv, lv_smem);
+        if (rc) return rc;
         k_gradients_lv<<<n_redz, 32 * LV_WARPS, lv_smem, st>>>(P, dens, n_redz, vals, grads, d_status);
     } else {
         k_gradients<<<n_redz, 256, 0, st>>>(P, dens, n_redz, vals, grads, d_status);

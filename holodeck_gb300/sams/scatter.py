@@ -83,6 +83,9 @@ class DevicePlan:
         s.grad_tol = GRAD_TOL
         s.grad_maxiter = GRAD_MAXITER
         self.struct = s
+        # the copies ran on this thread's stream; the plan is shared through the cache with workers on
+        # other streams, so it is complete before anyone can find it there
+        t.cuda.current_stream(D.device(dev)).synchronize()
 
 
 def device_plan(mtot, mrat, scatter, refine=4):
