@@ -412,6 +412,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+DEVICE_BATCH = 16
 BATCH_CONFIG = ("batched library: Latin-hypercube samples (seed 0) of PS_Classic_Phenom_Uniform (gsmf_phi0, "
                 "gsmf_mchar0_log10, mmb_mamp_log10, mmb_scatter_dex, hard_time, hard_gamma_inner), per-sample grid "
                 "uniform integers in [40, 91] per axis and realizations in [100, 1000] (default_rng(0)), "
@@ -431,6 +432,14 @@ def run_batched(args, rank=0, world=1):
                             indices=batch.shard_indices(n, rank, world), stats=stats, precision=args.precision)
     job = batch.reduce_stats(stats)                       # max wall time, summed work over the replicas
     wall, reals, draws = job["seconds"], job["realizations"], job["draws"]
+    # the same library with the realizations of DEVICE_BATCH samples per kernel launch, on the
+    # schedule found above (the results are identical; only the wall time is compared)
+    dstats = {}
+    batch.run_library(space, shapes, nreals, nfreqs=NFREQ, nloudest=NLOUD, seed=1,
+                      indices=batch.shard_indices(n, rank, world), stats=dstats, precision=args.precision,
+                      workers=stats["workers"], waves=stats["waves"], tune=False, batch=DEVICE_BATCH,
+                      reduce=lambda r: None)
+    djob = batch.reduce_stats(dstats)
     d2h = sum(sum(v.nbytes for k, v in r.items() if isinstance(v, np.ndarray)) for r in out if r is not None)
     tuning = stats.get("tuning") or {}
     table = tuning.get("table", {})
@@ -443,7 +452,12 @@ def run_batched(args, rank=0, world=1):
             "autotune_draws_per_s": table,
             "speedup_vs_one_worker_in_probe": (best / one) if (best and one) else None,
             "e2e": "host parameters in, host hc_ss / hc_bg out; per-sample scatter plans built on the host "
-                   "inside the timed region", "d2h_bytes": int(d2h)}
+                   "inside the timed region", "d2h_bytes": int(d2h),
+            "errors": dict(list(stats.get("errors", {}).items())[:3]),
+            "device_batched": {"batch": DEVICE_BATCH, "blocks_per_sm": 0, "seconds": djob["seconds"],
+                               "draws_per_s": djob["draws"] / djob["seconds"], "failed": djob["failed"],
+                               "note": "realizations of up to batch samples per k_bulk_multi launch (one block "
+                                       "per work item), grid stages on the same worker pool"}}
 
 
 EMU_CONFIG = ("learned emulator: 4-member ensemble of MLPs 6 -> 4x256 (SiLU) -> 40 x (5/50/95th percentile "

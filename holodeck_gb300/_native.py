@@ -80,6 +80,11 @@ class HgbScatterPlan(ctypes.Structure):
                 [("grad_tol", _d), ("grad_maxiter", _i)])
 
 
+class HgbLoudestSample(ctypes.Structure):
+    _fields_ = [("number", _p), ("h2fdf", _p), ("order", _p), ("n_bins", _l), ("nreals", _i), ("seed", _u64),
+                ("hc2ss", _p), ("hc2bg", _p), ("workspace", _p), ("workspace_bytes", _sz), ("d_status", _p)]
+
+
 MLP_MAX_LAYERS = 8       # HGB_MLP_MAX_LAYERS
 MLP_SPLIT_ROWS = 128     # HGB_MLP_SPLIT_ROWS
 
@@ -123,6 +128,8 @@ SIGNATURES = [
     ("hgb_loudest_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
     ("hgb_loudest_hc_from_sorted", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p]),
     ("hgb_loudest_hc_from_sorted_ex", _i, [_p, _p, _l, _i, _i, _i, _p, _i, _u64, _p, _p, _p, _p, _sz, _p, _p, _i]),
+    ("hgb_loudest_batch_workspace_bytes", _sz, [ctypes.POINTER(HgbLoudestSample), _i, _i]),
+    ("hgb_loudest_hc_batch", _i, [ctypes.POINTER(HgbLoudestSample), _i, _i, _i, _i, _p, _sz, _p]),
     ("hgb_param_grids", _i, [_p, _i, _i, _i, _p, _i, _p, _d, ctypes.POINTER(HgbCosmo), _p, _p, _p, _p, _p, _p,
                              _p]),
     ("hgb_loudest_par_workspace_bytes", _sz, [_l, _i, _i, _i, _i]),
@@ -213,6 +220,12 @@ def launch_count():
 
 def add_launches(n):
     """Count kernels of a call whose launch count depends on its arguments."""
+    with _launch_lock:
+        _launches[0] += int(n)
+
+
+def note_launches(n):
+    """Count ``n`` kernel launches made by an entry point whose count depends on its arguments."""
     with _launch_lock:
         _launches[0] += int(n)
 

@@ -66,6 +66,9 @@
 
 #include <atomic>
 
+#include <algorithm>
+#include <vector>
+
 #include "hgb_common.cuh"
 
 namespace {
@@ -902,18 +905,29 @@ __device__ __forceinline__ void add_par(float *psm, int sl, int t, int j, float 
     }
 }
 
+// Shared state of one k_bulk block (static shared memory of the kernels that run bulk_block).
+template <bool PARAMS>
+struct BulkShared {
+    Tile s;
+    typename std::conditional<PARAMS, SlotsKahan, SlotsPlain>::type st;
+    int q_min_s, q_max_s;
+};
+
+// One k_bulk block's work: chunk c (tiles c, c + nchunk, ...) of frequency f for the realizations of
+// group rg (rg * RB * RPT + thread + i * RB, i < RPT), written to part[c][f][r].  Every shared word it
+// reads it first writes, so a block may run it for several (c, f, rg) in turn.
 template <bool SORTED, bool PARAMS>
-__global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
-                                                          const double *__restrict__ h_in,
-                                                          const int *__restrict__ qpos, double *__restrict__ part,
-                                                          int *d_status) {
-    __shared__ Tile s;
-    __shared__ typename std::conditional<PARAMS, SlotsKahan, SlotsPlain>::type st;
-    extern __shared__ float psm[];   // PARAMS only: PAR_SMEM bytes
-    __shared__ int q_min_s, q_max_s;
-    const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+__device__ __forceinline__ void bulk_block(const BulkArgs &a, const ParArgs &pa, const double *__restrict__ lam_in,
+                                           const double *__restrict__ h_in, const int *__restrict__ qpos,
+                                           double *__restrict__ part, int *d_status, const int c, const int f,
+                                           const int rg, BulkShared<PARAMS> &sh, float *psm) {
+    Tile &s = sh.s;
+    auto &st = sh.st;
+    int &q_min_s = sh.q_min_s;
+    int &q_max_s = sh.q_max_s;
+    const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
-    const int r0 = blockIdx.z * RB * RPT + t;
+    const int r0 = rg * RB * RPT + t;
     int rpt = 0;   // realizations of this thread: r0 + i * RB, i < rpt
     while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
     // register accumulators for the passes with a fixed realization slot
@@ -1273,7 +1287,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(Bu
             // a realization sees a few events per tile).  Each thread then folds its slots into its
             // Kahan sums.
             unsigned long long *sub = reinterpret_cast<unsigned long long *>(s.u.arena);   // [RPT * RB]
-            const int nr_blk = min(RB * RPT, a.nr - (int)blockIdx.z * RB * RPT);
+            const int nr_blk = min(RB * RPT, a.nr - rg * RB * RPT);
             int runs = 0, e_hs = -1000;
             if (t < n_sparse) {
                 const int js = s.list[KIND_SPARSE][t];
@@ -1321,7 +1335,7 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(Bu
                 const int re = min((run + 1) << lg, nr_blk);
                 const float lf = s.lamf[j], hs = s.hs[j];
                 const int pos = s.pos[j];
-                const uint4 ctr = make_uint4((uint32_t)pos, ((uint32_t)blockIdx.z << 7) | (uint32_t)run,
+                const uint4 ctr = make_uint4((uint32_t)pos, ((uint32_t)rg << 7) | (uint32_t)run,
                                              (uint32_t)(f + a.f_offset), a.domain | W_SPARSE);
                 int r = run << lg;   // the next gap counts from here
                 // every event advances r, so a run takes at most 2^lg + 1 steps
@@ -1384,21 +1398,73 @@ __global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(Bu
     }
 }
 
+// grid (nchunk, nf, realization groups): block (c, f, rg) runs bulk_block for itself
+template <bool SORTED, bool PARAMS>
+__global__ void __launch_bounds__(RB, PARAMS ? 2 : BULK_BLOCKS_PER_SM) k_bulk(BulkArgs a, ParArgs pa, const double *__restrict__ lam_in,
+                                                          const double *__restrict__ h_in,
+                                                          const int *__restrict__ qpos, double *__restrict__ part,
+                                                          int *d_status) {
+    __shared__ BulkShared<PARAMS> sh;
+    extern __shared__ float psm[];   // PARAMS only: PAR_SMEM bytes
+    bulk_block<SORTED, PARAMS>(a, pa, lam_in, h_in, qpos, part, d_status, blockIdx.x, blockIdx.y, blockIdx.z, sh, psm);
+}
+
+// ---- 4c. many samples in one launch.  A sample's realization stage is the (chunk, frequency,
+// realization group) blocks of its own k_bulk grid; the work list names them as items
+// (sample, c, f, rg), and k_bulk_multi runs bulk_block for each item.  With `next` a block takes
+// items from the counter until the list is exhausted (a persistent grid of a few blocks per SM);
+// without it block i runs item i.  Each item computes exactly what block (c, f, rg) of the sample's
+// own k_bulk launch computes, so a sample's partials do not depend on the batch around it.
+struct BulkJob {
+    BulkArgs a;
+    const double *lam, *h;
+    const int *q;
+    double *part;
+    int *status;
+};
+
+__global__ void __launch_bounds__(RB, BULK_BLOCKS_PER_SM) k_bulk_multi(const BulkJob *__restrict__ jobs,
+                                                                       const int4 *__restrict__ items, int n_items,
+                                                                       int *next) {
+    __shared__ BulkShared<false> sh;
+    __shared__ int s_item;
+    int it = next ? -1 : (int)blockIdx.x;
+    while (true) {
+        if (next) {
+            __syncthreads();   // the previous item is finished with the shared state
+            if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
+            __syncthreads();
+            it = s_item;
+        }
+        if (it >= n_items) break;
+        const int4 w = items[it];
+        const BulkJob &J = jobs[w.x];   // read where used (L1), not held in registers
+        bulk_block<true, false>(J.a, ParArgs{}, J.lam, J.h, J.q, J.part, J.status, w.y, w.z, w.w, sh, nullptr);
+        if (!next) break;
+    }
+}
+
 // ---- 4b. bins above PTRS32_MAX (PTRS64 / Normal in FP64) when k_bulk leaves them out: the same
 // grid, chunks and realizations as k_bulk, run after it on the same stream; each block adds its
 // wide bins' sums (FP64, bin order) to the partials k_bulk wrote, and blocks without wide bins
 // write nothing.
+struct WideShared {
+    double w_lam[RB], w_h[RB];
+    int w_pos[RB];
+    int w_count[NWARP];
+};
+
 template <bool SORTED>
-__global__ void __launch_bounds__(RB) k_bulk_wide(BulkArgs a, const double *__restrict__ lam_in,
-                                                   const double *__restrict__ h_in, const int *__restrict__ qpos,
-                                                   double *__restrict__ part, int *d_status) {
-    __shared__ double w_lam[RB], w_h[RB];
-    __shared__ int w_pos[RB];
-    __shared__ int w_count[NWARP];
+__device__ __forceinline__ void wide_block(const BulkArgs &a, const double *__restrict__ lam_in,
+                                           const double *__restrict__ h_in, const int *__restrict__ qpos,
+                                           double *__restrict__ part, int *d_status, const int c, const int f,
+                                           const int rg, WideShared &sh) {
+    double *w_lam = sh.w_lam, *w_h = sh.w_h;
+    int *w_pos = sh.w_pos, *w_count = sh.w_count;
     if (*(volatile int *)a.wide_flag == 0) return;   // k_bulk met no such bin (uniform over the grid)
-    const int c = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+    const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
-    const int r0 = blockIdx.z * RB * RPT + t;
+    const int r0 = rg * RB * RPT + t;
     int rpt = 0;
     while (rpt < RPT && r0 + rpt * RB < a.nr) rpt++;
     const int *q_row = SORTED ? qpos + (long)f * a.nr + r0 : nullptr;
@@ -1455,6 +1521,26 @@ __global__ void __launch_bounds__(RB) k_bulk_wide(BulkArgs a, const double *__re
 #pragma unroll
     for (int i = 0; i < RPT; i++)
         if (i < rpt) part[((long)c * a.nf + f) * a.nr + r0 + (long)i * RB] += acc[i];
+}
+
+template <bool SORTED>
+__global__ void __launch_bounds__(RB) k_bulk_wide(BulkArgs a, const double *__restrict__ lam_in,
+                                                   const double *__restrict__ h_in, const int *__restrict__ qpos,
+                                                   double *__restrict__ part, int *d_status) {
+    __shared__ WideShared sh;
+    wide_block<SORTED>(a, lam_in, h_in, qpos, part, d_status, blockIdx.x, blockIdx.y, blockIdx.z, sh);
+}
+
+// the wide pass of the items of a work list, grid-stride over the items
+__global__ void __launch_bounds__(RB) k_bulk_wide_multi(const BulkJob *__restrict__ jobs,
+                                                        const int4 *__restrict__ items, int n_items) {
+    __shared__ WideShared sh;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const int4 w = items[it];
+        const BulkJob &J = jobs[w.x];
+        wide_block<true>(J.a, J.lam, J.h, J.q, J.part, J.status, w.y, w.z, w.w, sh);
+        __syncthreads();   // the shared lists are rewritten by the next item
+    }
 }
 
 // ---- 5. background = prefix remainder + chunk partials (fixed order)
@@ -1747,6 +1833,141 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
     if ((rc = hgb::check_launch())) return rc;
     k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(a.nchunk, nfr, bgp, part, hc2bg);
     return hgb::check_launch();
+}
+
+size_t hgb_loudest_batch_workspace_bytes(const hgb_loudest_sample *samples, int n_samples, int n_freq) {
+    if (!samples || n_samples <= 0 || n_freq <= 0) return 0;
+    size_t items = 0;
+    for (int i = 0; i < n_samples; i++) {
+        const hgb_loudest_sample &S = samples[i];
+        if (S.n_bins <= 0 || S.nreals <= 0) continue;
+        items += (size_t)choose_nchunk(S.n_bins, n_freq, S.nreals, HGB_BULK_WAVES_MAX) * n_freq * n_rgroups(S.nreals);
+    }
+    return align256(sizeof(BulkJob) * n_samples) + align256(sizeof(int) * n_samples) + align256(sizeof(int4) * items) +
+           256;
+}
+
+int hgb_loudest_hc_batch(const hgb_loudest_sample *samples, int n_samples, int n_freq, int nloud, int blocks_per_sm,
+                         void *workspace, size_t workspace_bytes, void *stream) {
+    HGB_CHECK_ARG(samples && n_samples >= 0 && n_freq >= 1 && n_freq <= 65535 && nloud >= 0 && nloud <= 255);
+    HGB_CHECK_ARG(blocks_per_sm >= 0 && blocks_per_sm <= BULK_BLOCKS_PER_SM);
+    for (int i = 0; i < n_samples; i++) {
+        const hgb_loudest_sample &S = samples[i];
+        HGB_CHECK_ARG(S.number && S.h2fdf && S.order && S.hc2bg && (nloud == 0 || S.hc2ss));
+        HGB_CHECK_ARG(S.n_bins >= 0 && S.n_bins < (1L << 31) - 1 && S.nreals >= 0 && S.nreals <= HGB_MAX_NREALS);
+        if (S.n_bins > 0 && S.nreals > 0 &&
+            (!S.workspace ||
+             S.workspace_bytes < hgb_loudest_workspace_bytes(S.n_bins, n_freq, S.nreals, nloud, HGB_RNG_PHILOX)))
+            return HGB_ERR_WORKSPACE;
+    }
+    if (n_samples == 0) return HGB_OK;
+    if (!workspace || workspace_bytes < hgb_loudest_batch_workspace_bytes(samples, n_samples, n_freq))
+        return HGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int waves = bulk_waves();
+    char *w = (char *)workspace;
+    BulkJob *d_jobs = (BulkJob *)w;
+    w += align256(sizeof(BulkJob) * n_samples);
+    int *d_flags = (int *)w;
+    w += align256(sizeof(int) * n_samples);
+    int4 *d_items = (int4 *)w;
+    std::vector<BulkJob> jobs;
+    std::vector<int> job_sample;
+    std::vector<int> nchunk;
+    int rc;
+    // per sample: the gather into loudest-first order, the exact scan and the loudest slots, as
+    // hgb_loudest_hc_from_sorted does
+    for (int i = 0; i < n_samples; i++) {
+        const hgb_loudest_sample &S = samples[i];
+        if (S.nreals == 0) continue;
+        if (S.n_bins == 0) {
+            if (nloud) cudaMemsetAsync(S.hc2ss, 0, sizeof(double) * (size_t)n_freq * S.nreals * nloud, st);
+            cudaMemsetAsync(S.hc2bg, 0, sizeof(double) * (size_t)n_freq * S.nreals, st);
+            if ((rc = hgb::check_launch())) return rc;
+            continue;
+        }
+        const LoudLayout L = loud_layout(S.n_bins, n_freq, S.nreals, HGB_RNG_PHILOX, waves);
+        char *sw = (char *)S.workspace;
+        double *lam_s = (double *)(sw + L.off_lam);
+        double *h_s = (double *)(sw + L.off_h);
+        launch_gather_sorted(S.number, S.h2fdf, S.order, S.n_bins, n_freq, lam_s, h_s, st);
+        if ((rc = hgb::check_launch())) return rc;
+        double *cum = (double *)(sw + L.off_cum);
+        int *q = (int *)(sw + L.off_q);
+        double *bgp = (double *)(sw + L.off_bgp);
+        if ((rc = cumulate(S.n_bins, n_freq, lam_s, nullptr, (double *)(sw + L.off_seg), cum, st))) return rc;
+        PrefixArgs pa;
+        pa.nb = S.n_bins;
+        pa.nf = n_freq;
+        pa.nr = S.nreals;
+        pa.nl = nloud;
+        pa.f_offset = 0;
+        pa.key = make_key(S.seed);
+        const long nfr = (long)n_freq * S.nreals;
+        k_loud_prefix<false><<<(unsigned)hgb::ceil_div(nfr, 128), 128, 0, st>>>(pa, ParArgs{}, lam_s, h_s, cum,
+                                                                                S.hc2ss, bgp, q, S.d_status);
+        if ((rc = hgb::check_launch())) return rc;
+        BulkJob J;
+        J.a = bulk_args(S.n_bins, n_freq, S.nreals, L.nchunk, S.seed, 0u, 0);
+        J.a.wide_flag = d_flags + jobs.size();
+        J.lam = lam_s;
+        J.h = h_s;
+        J.q = q;
+        J.part = (double *)(sw + L.off_part);
+        J.status = S.d_status;
+        jobs.push_back(J);
+        job_sample.push_back(i);
+        nchunk.push_back(L.nchunk);
+    }
+    const int nj = (int)jobs.size();
+    if (nj == 0) return HGB_OK;
+    // the work list: frequency by frequency (the low frequencies hold most occupied bins, so the
+    // costly items come first), within a frequency the samples with the most bins per chunk first
+    std::vector<int> by_size(nj);
+    for (int j = 0; j < nj; j++) by_size[j] = j;
+    std::sort(by_size.begin(), by_size.end(), [&](int x, int y) {
+        const long bx = jobs[x].a.nb / nchunk[x], byy = jobs[y].a.nb / nchunk[y];
+        return bx != byy ? bx > byy : x < y;
+    });
+    std::vector<int4> items;
+    for (int f = 0; f < n_freq; f++)
+        for (int j : by_size)
+            for (int rg = 0; rg < n_rgroups(jobs[j].a.nr); rg++)
+                for (int c = 0; c < nchunk[j]; c++) items.push_back(make_int4(j, c, f, rg));
+    const int n_items = (int)items.size();
+    int *d_next = (int *)(w + align256(sizeof(int4) * items.size()));
+    // pageable host sources: each copy is staged before the call returns, so the vectors may go
+    cudaError_t err = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(BulkJob) * nj, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(d_flags, 0, sizeof(int) * nj, st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(d_next, 0, sizeof(int), st);
+    if (err != cudaSuccess) {
+        hgb::set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    if ((rc = bulk_event(0, st))) return rc;
+    if (blocks_per_sm > 0) {
+        const long grid = std::min((long)n_items, (long)hgb::sm_count() * blocks_per_sm);
+        k_bulk_multi<<<(unsigned)grid, RB, 0, st>>>(d_jobs, d_items, n_items, d_next);
+    } else {
+        k_bulk_multi<<<(unsigned)n_items, RB, 0, st>>>(d_jobs, d_items, n_items, nullptr);
+    }
+    if ((rc = hgb::check_launch())) return rc;
+    if ((rc = bulk_event(1, st))) return rc;
+    const long wgrid = std::min((long)n_items, (long)hgb::sm_count() * 8);
+    k_bulk_wide_multi<<<(unsigned)wgrid, RB, 0, st>>>(d_jobs, d_items, n_items);
+    if ((rc = hgb::check_launch())) return rc;
+    for (int j = 0; j < nj; j++) {
+        const hgb_loudest_sample &S = samples[job_sample[j]];
+        const LoudLayout L = loud_layout(S.n_bins, n_freq, S.nreals, HGB_RNG_PHILOX, waves);
+        const long nfr = (long)n_freq * S.nreals;
+        char *sw = (char *)S.workspace;
+        k_bg_reduce<<<(unsigned)hgb::ceil_div(nfr, 256), 256, 0, st>>>(L.nchunk, nfr, (double *)(sw + L.off_bgp),
+                                                                       (double *)(sw + L.off_part), S.hc2bg);
+        if ((rc = hgb::check_launch())) return rc;
+    }
+    return HGB_OK;
 }
 
 size_t hgb_loudest_par_workspace_bytes(long n_bins, int n_freq, int nreals, int nloud, int mode) {

@@ -99,6 +99,49 @@ def loudest_device(number, h2fdf, nreals, nloudest, order, seed=None, replay=Non
     return hc2ss, hc2bg
 
 
+def loudest_batch_device(samples, nloudest, blocks_per_sm=0):
+    """:func:`loudest_device` (Philox draws) for many samples in one bulk-background launch
+    (``hgb_loudest_hc_batch``).  ``samples``: list of dicts with ``number`` and ``h2fdf`` (B_i, F)
+    device tensors (F shared), ``order`` (B_i,) int32, ``nreals``, ``seed`` and ``status`` (a
+    :class:`_device.StatusWord` or None).  Returns [(hc2ss (F, R_i, L), hc2bg (F, R_i))], each equal
+    to that sample's own :func:`loudest_device` result with the same seed, bit for bit.
+    ``blocks_per_sm``: 0 = one block per work item, 1..6 = a persistent grid (see the C header)."""
+    t = D.torch()
+    if not samples:
+        return []
+    nf = int(samples[0]["number"].shape[-1])
+    dev = samples[0]["number"].device
+    arr = (N.HgbLoudestSample * len(samples))()
+    outs, keep = [], []
+    lib = N.load()
+    for ii, smp in enumerate(samples):
+        num, hh, order = smp["number"], smp["h2fdf"], smp["order"]
+        nr = int(smp["nreals"])
+        if int(num.shape[-1]) != nf or tuple(hh.shape) != tuple(num.shape) or num.device != dev:
+            raise ValueError("every sample's number / h2fdf must be (B, F) on one device with the same F")
+        nb = int(num.numel() // nf)
+        if order.dtype != t.int32 or int(order.numel()) != nb or order.device != dev:
+            raise ValueError(f"order must be an int32 tensor of {nb} bin indices on {dev} (see checked_order)")
+        hc2ss = t.empty((nf, nr, int(nloudest)), dtype=t.float64, device=dev)
+        hc2bg = t.empty((nf, nr), dtype=t.float64, device=dev)
+        ws_bytes = lib.hgb_loudest_workspace_bytes(nb, nf, nr, int(nloudest), N.RNG_PHILOX)
+        ws = D.workspace(ws_bytes, dev)
+        st = smp.get("status")
+        seed = new_seed() if smp.get("seed") is None else int(smp["seed"]) & 0xFFFFFFFFFFFFFFFF
+        arr[ii] = N.HgbLoudestSample(num.data_ptr(), hh.data_ptr(), order.data_ptr(), nb, nr, seed,
+                                     hc2ss.data_ptr(), hc2bg.data_ptr(), ws.data_ptr(), int(ws_bytes),
+                                     st.t.data_ptr() if st is not None else None)
+        outs.append((hc2ss, hc2bg))
+        keep.append(ws)
+    bw_bytes = lib.hgb_loudest_batch_workspace_bytes(arr, len(samples), nf)
+    bw = D.workspace(bw_bytes, dev)
+    N.call("hgb_loudest_hc_batch", arr, len(samples), nf, int(nloudest), int(blocks_per_sm), N.ptr(bw),
+           int(bw_bytes), N.stream_handle())
+    N.note_launches(5 * len(samples) + 2)
+    del keep   # the caching allocator reuses the workspaces only after this stream's work
+    return outs
+
+
 def loudest_hc_from_sorted(number, h2fdf, nreals, nloudest, msort, qsort, zsort, normal_threshold=1e10,
                            seed=None, replay=None):
     """hc^2 of the loudest sources (F, R, L) and of the background (F, R); cyutils.pyx:1220-1264."""

@@ -32,7 +32,8 @@ import numpy as np
 from .. import _device as D
 from .. import _native as N
 from . import DEF_NUM_FBINS, DEF_NUM_LOUDEST, DEF_PTA_DUR
-from .lib_tools import run_model
+from .. import single_sources
+from .lib_tools import run_model, run_model_grids
 
 _TUNING_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "_build", "tuning.json")
 _TUNING_LOCK = threading.Lock()
@@ -155,12 +156,18 @@ def _save_sim_file(path, space, job, res, err):
 
 
 def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=None, output_dir=None,
-              max_failures=None):
+              max_failures=None, batch=0, blocks_per_sm=0):
     """Run ``jobs`` on ``workers`` host threads, one CUDA stream each; returns {index: result or None}
     and {index: exception} for samples that failed.  A result is run_model's dict, or ``reduce`` of it.
     With ``output_dir`` every sample also writes its file there as it finishes.  With ``max_failures``
     the workers stop taking samples once more than that many have failed, and RuntimeError is raised
-    (gen_lib.py:213-218)."""
+    (gen_lib.py:213-218).
+
+    ``batch`` > 0 (single-source realizations without parameters only): the workers run each
+    sample's grid stages (:func:`lib_tools.run_model_grids`) and hand the finished grids to one
+    realization thread, which launches the bulk backgrounds of up to ``batch`` samples at a time as
+    one kernel (:func:`single_sources.ss_realize_batch_device`, ``blocks_per_sm`` as there).  The
+    results equal run_model's, bit for bit."""
     t = D.torch()
     dev = D.device()
     order = sorted(jobs, key=lambda j: -j.cost(nfreqs))
@@ -171,6 +178,22 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
     lock = threading.Lock()
     stop = threading.Event()
     streams = [t.cuda.Stream(device=dev) for _ in range(workers)]
+    batched = batch > 0 and flags.get("singles_flag", True) and not flags.get("params_flag", False)
+    ready = queue.Queue(maxsize=max(2 * batch, 1)) if batched else None
+    _DONE = object()
+
+    def finish(job, res, err):
+        if output_dir is not None:
+            try:
+                _save_sim_file(sim_fname(output_dir, job.index), space, job, res, err)
+            except OSError as exc:
+                err = err or exc
+        with lock:
+            results[job.index] = None if err is not None else (res if reduce is None else reduce(res))
+            if err is not None:
+                errors[job.index] = err
+                if max_failures is not None and len(errors) > max_failures:
+                    stop.set()
 
     def work(stream):
         with t.cuda.stream(stream):
@@ -178,27 +201,64 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
                 try:
                     job = q.get_nowait()
                 except queue.Empty:
-                    return
+                    break
                 res = err = None
                 try:
                     sam, hard = space.model_for_params(job.params, job.shape)
+                    if batched:
+                        data, _, number, h2fdf = run_model_grids(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs,
+                                                                 nreals=job.nreals, seed=job.seed, **flags)
+                        ev = t.cuda.Event()
+                        ev.record(stream)
+                        ready.put((job, data, number, h2fdf, ev))
+                        continue
                     res = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
                                     nloudest=nloudest, seed=job.seed, **flags)
                 except Exception as exc:   # a failed sample gives NaN rows, as in the reference's libraries
                     err = exc
-                if output_dir is not None:
-                    try:
-                        _save_sim_file(sim_fname(output_dir, job.index), space, job, res, err)
-                    except OSError as exc:
-                        err = err or exc
-                with lock:
-                    results[job.index] = None if err is not None else (res if reduce is None else reduce(res))
-                    if err is not None:
-                        errors[job.index] = err
-                        if max_failures is not None and len(errors) > max_failures:
-                            stop.set()
+                finish(job, res, err)
+        if batched:
+            ready.put(_DONE)
+
+    def realize():
+        rstream = t.cuda.Stream(device=dev)
+        live = workers
+        with t.cuda.stream(rstream):
+            while live > 0:
+                group = []
+                while len(group) < batch and live > 0:
+                    item = ready.get()
+                    if item is _DONE:
+                        live -= 1
+                    else:
+                        group.append(item)
+                if not group:
+                    continue
+                done = set()
+                try:
+                    for _, _, number, h2fdf, ev in group:
+                        rstream.wait_event(ev)
+                        number.record_stream(rstream)   # made on a worker's stream, read on this one
+                        h2fdf.record_stream(rstream)
+                    outs = single_sources.ss_realize_batch_device(
+                        [(number, h2fdf, job.nreals, job.seed) for job, _, number, h2fdf, _ in group], nloudest,
+                        blocks_per_sm=blocks_per_sm)
+                    for (job, data, _, _, _), out in zip(group, outs):
+                        if isinstance(out, Exception):
+                            res, err = None, out
+                        else:
+                            res, err = dict(data, hc_ss=D.to_host(out[0]), hc_bg=D.to_host(out[1])), None
+                        done.add(job.index)
+                        finish(job, res, err)
+                except Exception as exc:   # the whole group fails; the workers keep going
+                    for job, *_ in group:
+                        if job.index not in done:
+                            finish(job, None, exc)
+        rstream.synchronize()
 
     threads = [threading.Thread(target=work, args=(s,), daemon=True) for s in streams]
+    if batched:
+        threads.append(threading.Thread(target=realize, daemon=True))
     for th in threads:
         th.start()
     for th in threads:
@@ -288,7 +348,7 @@ def autotune(space, jobs, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST, pta_du
 def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=DEF_NUM_LOUDEST,
                 pta_dur=DEF_PTA_DUR, seed=0, singles_flag=True, gwb_flag=False, params_flag=False,
                 details_flag=False, workers=None, waves=None, tune=True, indices=None, stats=None, reduce=None,
-                output_dir=None, recreate=False, max_failures=None, precision="fp64"):
+                output_dir=None, recreate=False, max_failures=None, precision="fp64", batch=0, blocks_per_sm=0):
     """Evaluate the samples of ``space`` (all, or ``indices``) on this GPU; returns the list of
     per-sample :func:`lib_tools.run_model` dicts in sample order (``None`` for a failed sample), the
     input that :func:`lib_tools.write_library` takes.
@@ -306,7 +366,9 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
     file exists and is not a failure are loaded instead of run (unless ``recreate``), failed ones are
     attempted again (gen_lib.py:288-300).  ``max_failures``: raise RuntimeError once more samples than
     this have failed (gen_lib.py:42, :213-218).  ``precision``: the grid arithmetic of every sample
-    (see :meth:`Semi_Analytic_Model.gwb`).
+    (see :meth:`Semi_Analytic_Model.gwb`).  ``batch`` / ``blocks_per_sm``: run the single-source
+    realizations of up to ``batch`` samples as one kernel launch (see :func:`_run_jobs`); the results
+    do not change.
     """
     flags = dict(singles_flag=singles_flag, gwb_flag=gwb_flag, params_flag=params_flag, details_flag=details_flag,
                  precision=precision)
@@ -347,13 +409,15 @@ def run_library(space, shapes=None, nreals=None, nfreqs=DEF_NUM_FBINS, nloudest=
         D.torch().cuda.synchronize()
         t0 = time.perf_counter()
         results, errors = _run_jobs(space, jobs, int(workers), nfreqs, nloudest, pta_dur, flags, reduce,
-                                    output_dir=output_dir, max_failures=max_failures)
+                                    output_dir=output_dir, max_failures=max_failures, batch=int(batch),
+                                    blocks_per_sm=int(blocks_per_sm))
         D.torch().cuda.synchronize()
         wall = time.perf_counter() - t0
     finally:
         N.check(lib.hgb_set_bulk_waves(old_waves), "hgb_set_bulk_waves")
     if stats is not None:
-        stats.update(workers=int(workers), waves=int(waves), seconds=wall, samples=len(jobs_all),
+        stats.update(workers=int(workers), waves=int(waves), batch=int(batch), blocks_per_sm=int(blocks_per_sm),
+                     seconds=wall, samples=len(jobs_all),
                      failed=len(errors), realizations=int(sum(j.nreals for j in jobs)),
                      draws=float(sum(j.cost(nfreqs) for j in jobs)), tuning=tuned,
                      errors={k: repr(v) for k, v in errors.items()})

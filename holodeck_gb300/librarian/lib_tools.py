@@ -229,6 +229,34 @@ def run_model(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_N
     ``gwb_flag`` ``gwb``.  ``seed`` (added) keys the Philox draws of the realizations; ``precision``
     (added) selects the grid arithmetic as in :meth:`Semi_Analytic_Model.gwb`.
     """
+    data, edges, number, h2fdf = run_model_grids(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=nreals,
+                                                 gwb_flag=gwb_flag, singles_flag=singles_flag,
+                                                 details_flag=details_flag, params_flag=params_flag, log=log,
+                                                 seed=seed, precision=precision)
+    if singles_flag or params_flag:
+        nloudest = nloudest if singles_flag else 1
+        s1 = None if seed is None else int(seed)
+        if params_flag:
+            hc_ss, hc_bg, sspar, bgpar = single_sources.ss_params_device(edges, data.pop('_redz_final_device'), number,
+                                                                         h2fdf, nreals, nloudest, seed=s1,
+                                                                         cosmo=sam._cosmo)
+            data['sspar'] = D.to_host(sspar)
+            data['bgpar'] = D.to_host(bgpar)
+        else:
+            hc_ss, hc_bg = single_sources.ss_realize_device(number, h2fdf, nreals, nloudest, seed=s1)
+        if singles_flag:
+            data['hc_ss'] = D.to_host(hc_ss)
+            data['hc_bg'] = D.to_host(hc_bg)
+    data.pop('_redz_final_device', None)
+    return data
+
+
+def run_model_grids(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_NUM_REALS, gwb_flag=True,
+                    singles_flag=True, details_flag=False, params_flag=False, log=None, seed=None, precision="fp64"):
+    """Everything of :func:`run_model` but the single-source realizations: returns (data, edges,
+    number, h2fdf) with ``data`` holding the frequencies, the details (``details_flag``) and ``gwb``
+    (``gwb_flag``), and number / h2fdf the device grids the realizations draw from.  With
+    ``params_flag`` data also carries the device redz_final under '_redz_final_device'."""
     if not any([gwb_flag, details_flag, singles_flag, params_flag]):
         err = f"No flags set!  {gwb_flag=} {details_flag=} {singles_flag=} {params_flag=}"
         if log is not None:
@@ -257,25 +285,14 @@ def run_model(sam, hard, pta_dur=DEF_PTA_DUR, nfreqs=DEF_NUM_FBINS, nreals=DEF_N
         data['num_params'] = [D.to_host(x) for x in num_pars]
         data['gwb_mtot_redz_final'] = D.to_host(gm)
         data['num_mtot_redz_final'] = D.to_host(nmr)
-    if singles_flag or params_flag:
-        nloudest = nloudest if singles_flag else 1
-        s1 = None if seed is None else int(seed)
-        if params_flag:
-            hc_ss, hc_bg, sspar, bgpar = single_sources.ss_params_device(edges, redz_final, number, h2fdf, nreals,
-                                                                         nloudest, seed=s1, cosmo=sam._cosmo)
-            data['sspar'] = D.to_host(sspar)
-            data['bgpar'] = D.to_host(bgpar)
-        else:
-            hc_ss, hc_bg = single_sources.ss_realize_device(number, h2fdf, nreals, nloudest, seed=s1)
-        if singles_flag:
-            data['hc_ss'] = D.to_host(hc_ss)
-            data['hc_bg'] = D.to_host(hc_bg)
     if gwb_flag:
         s2 = None if seed is None else (int(seed) ^ 0x5DEECE66D) & 0xFFFFFFFFFFFFFFFF
         gwb = gravwaves._gws_from_number_grid_integrated_redz(edges, redz_final, number, nreals, seed=s2,
                                                               cosmo=sam._cosmo)
         data['gwb'] = D.to_host(gwb)
-    return data
+    if params_flag:
+        data['_redz_final_device'] = redz_final
+    return data, edges, number, h2fdf
 
 
 def write_library(path, samples, sample_params, param_names, parameter_space_class_name="", gwb_only=False):

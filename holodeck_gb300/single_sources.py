@@ -47,6 +47,30 @@ def ss_realize_device(number, h2fdf, realize, loudest, seed=None, replay=None, o
     return hc2ss, hc2bg
 
 
+def ss_realize_batch_device(samples, loudest, blocks_per_sm=0):
+    """:func:`ss_realize_device` (Philox draws) for many samples, their bulk backgrounds in one launch.
+    ``samples``: list of (number, h2fdf, realize, seed), number / h2fdf (M_i-1, Q_i-1, Z_i-1, F) on
+    the current device with one F.  Returns one entry per sample: (hc_ss[F, R, L], hc_bg[F, R]), or
+    the exception that sample's status word raised (the others are unaffected)."""
+    items = []
+    for number, h2fdf, realize, seed in samples:
+        nf = int(number.shape[-1])
+        items.append(dict(number=number.reshape(-1, nf), h2fdf=h2fdf.reshape(-1, nf), order=sort_order_device(h2fdf),
+                          nreals=int(realize), seed=seed, status=D.StatusWord(number.device)))
+    outs = cyutils.loudest_batch_device(items, int(loudest), blocks_per_sm=blocks_per_sm)
+    res = []
+    for smp, (hc2ss, hc2bg) in zip(items, outs):
+        N.call("hgb_sqrt_inplace", N.ptr(hc2ss), int(hc2ss.numel()), N.stream_handle())
+        N.call("hgb_sqrt_inplace", N.ptr(hc2bg), int(hc2bg.numel()), N.stream_handle())
+    for smp, (hc2ss, hc2bg) in zip(items, outs):
+        try:
+            cyutils._raise_status(smp["status"])
+            res.append((hc2ss, hc2bg))
+        except RuntimeError as exc:
+            res.append(exc)
+    return res
+
+
 def param_grids_device(edges, redz, h2fdf=None, cosmo=None):
     """Device (redz_mid, dcom, sepa, angs), each (M-1, Q-1, Z-1, F), and the int32[4] frexp exponents of
     their largest finite magnitudes over the bins with nonzero strain (single_sources.py:117-143)."""

@@ -319,6 +319,37 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
                                   double *hc2ss, double *hc2bg, void *workspace, size_t workspace_bytes,
                                   int *d_status, void *stream, int freq_offset);
 
+/* hgb_loudest_hc_from_sorted (HGB_RNG_PHILOX, freq_offset 0) for many independent samples: the
+ * realization stage of a library, where librarian/lib_tools.py:714-842 (run_model) calls
+ * single_sources.ss_gws_redz -> cyutils.loudest_hc_from_sorted once per sample.  Each sample's
+ * gather, scan and loudest slots run as in the single call; the bulk background of every sample
+ * runs in ONE launch whose blocks take (sample, chunk, frequency, realization group) items from a
+ * device work list.  Every sample's hc2ss / hc2bg equal those of its own hgb_loudest_hc_from_sorted
+ * call with the same seed and the same hgb_set_bulk_waves setting, bit for bit.
+ * samples: HOST array; each entry's arrays are device pointers as in hgb_loudest_hc_from_sorted,
+ * all samples share n_freq and nloud, and each has its own workspace
+ * (hgb_loudest_workspace_bytes(n_bins, n_freq, nreals, nloud, HGB_RNG_PHILOX)) and status word.
+ * blocks_per_sm: 0 = one block per item (blocks retire as items finish, so kernels of other
+ * streams interleave); 1..6 = a persistent grid of that many blocks per SM, each taking items
+ * from an atomic counter.  workspace: hgb_loudest_batch_workspace_bytes(samples, ...) bytes for
+ * the work list, written before the launch. */
+typedef struct {
+    const double *number;      /* (n_bins, n_freq) */
+    const double *h2fdf;       /* (n_bins, n_freq) */
+    const int32_t *order;      /* (n_bins) loudest-first order */
+    long n_bins;
+    int nreals;
+    uint64_t seed;
+    double *hc2ss;             /* (n_freq, nreals, nloud) */
+    double *hc2bg;             /* (n_freq, nreals) */
+    void *workspace;
+    size_t workspace_bytes;
+    int *d_status;             /* may be NULL */
+} hgb_loudest_sample;
+size_t hgb_loudest_batch_workspace_bytes(const hgb_loudest_sample *samples, int n_samples, int n_freq);
+int hgb_loudest_hc_batch(const hgb_loudest_sample *samples, int n_samples, int n_freq, int nloud, int blocks_per_sm,
+                         void *workspace, size_t workspace_bytes, void *stream);
+
 /* Parameter grids of ss_gws_redz(params=True) (single_sources.py:117-143) on the (B, F) bins:
  * redz_mid = the redshift midpoints of redz_final along mtot, mrat, redz (-1 where <= 0),
  * dcom = comoving distance of redz_mid (+inf where it is -1), sepa = Kepler separation

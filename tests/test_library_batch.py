@@ -124,6 +124,54 @@ def test_batched_library_equals_per_sample_runs(built_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("blocks_per_sm", [0, 4])
+def test_batched_realizations_equal_per_sample_calls(built_lib, blocks_per_sm):
+    """One bulk launch over several samples' work items gives every sample's own loudest_device result
+    bit for bit: expectations from 1e-4 to 1e8 (every sampler regime, FP64 wide bins included),
+    different bin counts, realization counts across several groups of 1024."""
+    import torch
+    from holodeck_gb300 import cyutils, single_sources
+    from holodeck_gb300 import _device as D
+    rng = np.random.default_rng(21)
+    nf, nl = 3, 4
+    samples = []
+    for nb, nr in ((5000, 7), (20011, 1030), (777, 2100), (3, 1)):
+        lam = 10.0 ** rng.uniform(-4.0, 8.0, size=(nb, nf))
+        lam[rng.random((nb, nf)) < 0.3] = 0.0
+        h = 10.0 ** rng.uniform(-32.0, -26.0, size=(nb, nf))
+        num = torch.as_tensor(lam, device="cuda")
+        hh = torch.as_tensor(h, device="cuda")
+        samples.append(dict(number=num, h2fdf=hh, order=single_sources.sort_order_device(hh), nreals=nr,
+                            seed=1000 + nb, status=D.StatusWord()))
+    got = cyutils.loudest_batch_device(samples, nl, blocks_per_sm=blocks_per_sm)
+    for smp, (ss, bg) in zip(samples, got):
+        ref_ss, ref_bg = cyutils.loudest_device(smp["number"], smp["h2fdf"], smp["nreals"], nl, smp["order"],
+                                                seed=smp["seed"])
+        assert torch.equal(ss, ref_ss) and torch.equal(bg, ref_bg), smp["number"].shape
+        assert smp["status"].read() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("blocks_per_sm", [0, 3])
+def test_device_batched_library_equals_per_sample_runs(built_lib, blocks_per_sm):
+    """run_library with the realizations of up to four samples per launch gives each sample's
+    run_model result bit for bit (two launches for six samples)."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch, lib_tools
+    space = PS_Classic_Phenom_Uniform(nsamples=6, seed=2)
+    shapes, nreals = batch.random_shapes(6, lo=10, hi=18, reals_lo=5, reals_hi=1500, seed=4)
+    stats = {}
+    out = batch.run_library(space, shapes, nreals, nfreqs=5, nloudest=3, seed=11, workers=3, waves=2,
+                            gwb_flag=True, stats=stats, batch=4, blocks_per_sm=blocks_per_sm)
+    assert stats["failed"] == 0 and stats["batch"] == 4
+    for ii in range(6):
+        sam, hard = space.model_for_sample_number(ii, sam_shape=shapes[ii])
+        ref = lib_tools.run_model(sam, hard, nfreqs=5, nreals=nreals[ii], nloudest=3, gwb_flag=True,
+                                  seed=batch.sample_seed(11, ii))
+        for key in ("hc_ss", "hc_bg", "gwb", "fobs_edges"):
+            assert np.array_equal(out[ii][key], ref[key]), (ii, key)
+
+
+@pytest.mark.gpu
 def test_autotune_times_every_candidate(built_lib):
     from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
     from holodeck_gb300 import _native as N
