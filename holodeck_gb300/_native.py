@@ -87,6 +87,7 @@ class HgbLoudestSample(ctypes.Structure):
 
 MLP_MAX_LAYERS = 8       # HGB_MLP_MAX_LAYERS
 MLP_SPLIT_ROWS = 128     # HGB_MLP_SPLIT_ROWS
+MLP_FUSED_MAX_BATCH = 16 # HGB_MLP_FUSED_MAX_BATCH
 
 
 class HgbMlp(ctypes.Structure):
@@ -143,6 +144,7 @@ SIGNATURES = [
     ("hgb_mlp_param_count", _l, [ctypes.POINTER(HgbMlp)]),
     ("hgb_mlp_weight_count", _l, [ctypes.POINTER(HgbMlp)]),
     ("hgb_mlp_forward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _p]),
+    ("hgb_mlp_forward_fused", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p]),
     ("hgb_mlp_backward_workspace_bytes", _sz, [ctypes.POINTER(HgbMlp), _i]),
     ("hgb_mlp_backward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _l, _p, _p, _p, _sz, _p, _p]),
     ("hgb_mlp_adamw", _i, [ctypes.POINTER(HgbMlp), _p, _p, _p, _p, _p, _i, ctypes.c_float, ctypes.c_float,
@@ -204,7 +206,7 @@ KERNELS_PER_CALL = {
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_2pwl_phase_f32": 1, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_number_and_strain_f32": 1, "hgb_argsort_f0_desc": 25, "hgb_argsort_f0_desc_static": 25,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
-    "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1,
+    "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1, "hgb_mlp_forward_fused": 1,
 }
 _launches = [0]
 _launch_lock = threading.Lock()
@@ -220,12 +222,6 @@ def launch_count():
 
 def add_launches(n):
     """Count kernels of a call whose launch count depends on its arguments."""
-    with _launch_lock:
-        _launches[0] += int(n)
-
-
-def note_launches(n):
-    """Count ``n`` kernel launches made by an entry point whose count depends on its arguments."""
     with _launch_lock:
         _launches[0] += int(n)
 

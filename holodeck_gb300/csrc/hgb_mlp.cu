@@ -34,10 +34,14 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cooperative_groups.h>
+
 #include <atomic>
 #include <mutex>
 
 #include "hgb_common.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -658,6 +662,147 @@ int launch_gemm(const Op &op, int row_tiles, int members, int *status, cudaStrea
 
 const float *param_bias(const hgb_mlp *net, const NetView &v, int l) { return net->params + v.b_off[l]; }
 
+// ---- fused forward for small query batches --------------------------------------------------------
+// One cluster of FUSED_CL CTAs per member; CTA r of the cluster owns output columns
+// [r N_l / FUSED_CL, (r + 1) N_l / FUSED_CL) of every layer l.  At the start it bulk-copies its
+// column slice of every layer's weights (cp.async.bulk, one mbarrier per layer, so the later layers'
+// copies overlap the first layers' arithmetic) into shared memory.  A layer is a matrix-vector
+// product per query on the CUDA cores (a batch of at most FUSED_QMAX rows would leave a 128-row
+// tensor-core tile almost empty): each warp takes every fourth column, its lanes split the
+// reduction axis in runs of 8, fp32 products and a warp-shuffle sum.  The hidden activations
+// (bias, SiLU, rounded to bf16 as in the layered forward) are stored into the next activation
+// buffer of every CTA of the cluster (distributed shared memory), and one cluster barrier per layer
+// publishes them; the buffers alternate, so a CTA writing layer l + 1's inputs never meets a peer
+// still reading layer l's.  The last layer writes fp32 outputs.  The copies' waits are bounded: on
+// expiry the CTA flags HGB_STATUS_ITERATION_LIMIT and keeps taking part in every cluster barrier
+// (its outputs are not valid), and waits once more, bounded, for its copies before it returns.
+// The biases of all of the CTA's columns are loaded into shared memory at the start (one round trip
+// instead of one per column).  Inputs, outputs and the status word are read and written with plain
+// accesses, so they may be pinned host memory (device-accessible under unified addressing): a
+// graphed query then needs no copy nodes.  The status bit is set with a plain read-modify-write.
+constexpr int FUSED_CL = 8;
+constexpr int FUSED_QMAX = HGB_MLP_FUSED_MAX_BATCH;
+constexpr int FUSED_THREADS = 128;
+constexpr int FUSED_ACT_BYTES = FUSED_QMAX * WIDTH * 2;   // one bf16 activation buffer
+constexpr int FUSED_NCMAX = NMAX / FUSED_CL;              // columns per CTA and layer, at most
+
+struct FusedArgs {
+    int L, batch;
+    int K[HGB_MLP_MAX_LAYERS], N[HGB_MLP_MAX_LAYERS];
+    int w_smem[HGB_MLP_MAX_LAYERS];     // byte offset of layer l's weight slice in shared memory
+    long w_off[HGB_MLP_MAX_LAYERS], b_off[HGB_MLP_MAX_LAYERS];
+    long n_w, n_p;
+    const bf16 *weights;
+    const float *params;
+    const bf16 *x;
+    long x_es;
+    float *out;
+    int *status;
+};
+
+// global -> this CTA's shared memory, completion counted on mbar (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ float dot8_bf16(uint4 a, uint4 b, float acc) {
+    const __nv_bfloat162 *pa = reinterpret_cast<const __nv_bfloat162 *>(&a);
+    const __nv_bfloat162 *pb = reinterpret_cast<const __nv_bfloat162 *>(&b);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float2 fa = __bfloat1622float2(pa[i]), fb = __bfloat1622float2(pb[i]);
+        acc = fmaf(fa.x, fb.x, acc);
+        acc = fmaf(fa.y, fb.y, acc);
+    }
+    return acc;
+}
+
+__global__ void __cluster_dims__(FUSED_CL, 1, 1) __launch_bounds__(FUSED_THREADS)
+    k_mlp_fwd_fused(const __grid_constant__ FusedArgs a) {
+    extern __shared__ __align__(128) unsigned char fsm[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int e = blockIdx.y;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    bf16 *act0 = (bf16 *)fsm;
+    bf16 *act1 = (bf16 *)(fsm + FUSED_ACT_BYTES);
+    uint64_t *mbar = (uint64_t *)(fsm + 2 * FUSED_ACT_BYTES);
+    float *sbias = (float *)(fsm + 2 * FUSED_ACT_BYTES + 128);   // [layer][FUSED_NCMAX]
+    if (t == 0) {
+        for (int l = 0; l < a.L; l++) mbar_init(smem_u32(&mbar[l]), 1);
+    }
+    for (int i = t; i < a.L * FUSED_NCMAX; i += FUSED_THREADS) {
+        const int l = i / FUSED_NCMAX, n = i % FUSED_NCMAX, nc = a.N[l] / FUSED_CL;
+        if (n < nc) sbias[i] = __ldg(a.params + e * a.n_p + a.b_off[l] + rank * nc + n);
+    }
+    __syncthreads();
+    if (t == 0) {
+        for (int l = 0; l < a.L; l++) {
+            const int nc = a.N[l] / FUSED_CL;
+            const uint32_t bytes = (uint32_t)nc * (uint32_t)a.K[l] * 2u;
+            mbar_expect_tx(smem_u32(&mbar[l]), bytes);
+            bulk_g2s(smem_u32(fsm + a.w_smem[l]), a.weights + e * a.n_w + a.w_off[l] + (long)rank * nc * a.K[l], bytes,
+                     smem_u32(&mbar[l]));
+        }
+    }
+    const int Q = a.batch;
+    for (int i = t; i < Q * a.K[0]; i += FUSED_THREADS) {
+        const int q = i / a.K[0], k = i % a.K[0];
+        act0[q * WIDTH + k] = a.x[e * a.x_es + (long)q * a.K[0] + k];
+    }
+    cluster.sync();   // every CTA of the cluster runs before any stores into its shared memory
+    bool ok = true;
+    for (int l = 0; l < a.L; l++) {
+        const int K = a.K[l], N = a.N[l], nc = N / FUSED_CL, c0 = rank * nc;
+        if (ok && !mbar_wait(smem_u32(&mbar[l]), 0)) ok = false;
+        const bf16 *W = (const bf16 *)(fsm + a.w_smem[l]);   // [nc][K]
+        const bf16 *X = (l & 1) ? act1 : act0;
+        bf16 *Y = (l & 1) ? act0 : act1;
+        const float *bias = sbias + l * FUSED_NCMAX;
+        const bool last = l == a.L - 1;
+        for (int n = warp; n < nc; n += FUSED_THREADS / 32) {
+            const bf16 *wr = W + (long)n * K;
+            for (int q = 0; q < Q; q++) {
+                float acc = 0.0f;
+                for (int kc = lane; kc < K / 8; kc += 32)
+                    acc = dot8_bf16(*(const uint4 *)(wr + kc * 8), *(const uint4 *)(X + q * WIDTH + kc * 8), acc);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) {
+                    const float z = acc + bias[n];
+                    if (last) {
+                        a.out[((long)e * Q + q) * N + c0 + n] = z;
+                    } else {
+                        const bf16 y = __float2bfloat16_rn(silu(z));
+#pragma unroll
+                        for (int r = 0; r < FUSED_CL; r++) cluster.map_shared_rank(Y, r)[q * WIDTH + c0 + n] = y;
+                    }
+                }
+            }
+        }
+        cluster.sync();   // layer l + 1's inputs are in every CTA; layer l's are no longer read
+    }
+    if (!ok) {
+        if (t == 0) {
+            if (a.status) *(volatile int *)a.status |= HGB_STATUS_ITERATION_LIMIT;
+            for (int l = 0; l < a.L; l++) mbar_wait(smem_u32(&mbar[l]), 0);   // bounded: copies in flight
+        }
+        __syncthreads();
+    }
+}
+
+size_t fused_smem_bytes(const NetView &v, FusedArgs *fa) {
+    // two activation buffers, the mbarriers, the biases, then the weight slices
+    size_t off = 2 * (size_t)FUSED_ACT_BYTES + 128 + (((size_t)v.L * FUSED_NCMAX * 4 + 127) & ~(size_t)127);
+    for (int l = 0; l < v.L; l++) {
+        if (fa) fa->w_smem[l] = (int)off;
+        off += ((size_t)(v.N[l] / FUSED_CL) * v.K[l] * 2 + 127) & ~(size_t)127;
+    }
+    return off;
+}
+
 }  // namespace
 
 extern "C" {
@@ -701,6 +846,38 @@ int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride,
         if (rc) return rc;
     }
     return HGB_OK;
+}
+
+int hgb_mlp_forward_fused(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, float *out,
+                          int *d_status, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && net->params && net->weights && x && out && batch >= 0);
+    HGB_CHECK_ARG(x_member_stride >= 0 && batch <= HGB_MLP_FUSED_MAX_BATCH && net->n_members <= 65535);
+    HGB_CHECK_ARG(((uintptr_t)net->weights & 15) == 0);   // bulk-copy source alignment
+    if (batch == 0) return HGB_OK;
+    const NetView v = view_of(net);
+    FusedArgs fa{};
+    fa.L = v.L;
+    fa.batch = batch;
+    for (int l = 0; l < v.L; l++) {
+        fa.K[l] = v.K[l];
+        fa.N[l] = v.N[l];
+        fa.w_off[l] = v.w_off[l];
+        fa.b_off[l] = v.b_off[l];
+    }
+    fa.n_w = v.n_w;
+    fa.n_p = v.n_p;
+    fa.weights = (const bf16 *)net->weights;
+    fa.params = net->params;
+    fa.x = (const bf16 *)x;
+    fa.x_es = x_member_stride;
+    fa.out = out;
+    fa.status = d_status;
+    const size_t smem = fused_smem_bytes(v, &fa);
+    int rc = hgb::ensure_dyn_smem((const void *)k_mlp_fwd_fused, smem);
+    if (rc) return rc;
+    dim3 grid(FUSED_CL, (unsigned)v.E);
+    k_mlp_fwd_fused<<<grid, FUSED_THREADS, smem, (cudaStream_t)stream>>>(fa);
+    return hgb::check_launch();
 }
 
 size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch) {

@@ -137,7 +137,7 @@ def loudest_batch_device(samples, nloudest, blocks_per_sm=0):
     bw = D.workspace(bw_bytes, dev)
     N.call("hgb_loudest_hc_batch", arr, len(samples), nf, int(nloudest), int(blocks_per_sm), N.ptr(bw),
            int(bw_bytes), N.stream_handle())
-    N.note_launches(5 * len(samples) + 2)
+    N.add_launches(5 * len(samples) + 2)
     del keep   # the caching allocator reuses the workspaces only after this stream's work
     return outs
 

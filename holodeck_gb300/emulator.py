@@ -145,6 +145,21 @@ class MLPEnsemble:
         N.add_launches(self.L)
         return buf["out"]
 
+    def forward_fused(self, x, member_stride=0, owner=None):
+        """:meth:`forward` (inference) for at most ``_native.MLP_FUSED_MAX_BATCH`` rows in one launch
+        (hgb_mlp_forward_fused: weights and activations on chip, CUDA-core products).  The fp32 sums
+        run in another order than the tensor-core path's, so an activation can round to the
+        neighbouring bf16 value."""
+        t = D.torch()
+        assert x.dtype == t.bfloat16 and x.is_contiguous() and x.shape[-1] == self.dims[0]
+        batch = int(x.shape[-2])
+        if batch > N.MLP_FUSED_MAX_BATCH:
+            raise ValueError(f"the fused forward takes at most {N.MLP_FUSED_MAX_BATCH} rows, got {batch}")
+        buf = self._buffers_for(batch, False, ("fused", owner))
+        N.call("hgb_mlp_forward_fused", ctypes.byref(self.struct), N.ptr(x), int(member_stride), batch,
+               N.ptr(buf["out"]), self.status.ptr, N.stream_handle())
+        return buf["out"]
+
     def gradients(self, x, target):
         """Forward + backward of one batch: loss [E] (device) and self.grad [E, P]."""
         batch = int(x.shape[-2])
@@ -199,6 +214,7 @@ class Emulator:
         self.net = MLPEnsemble(dims, members=members, seed=seed, device=device)
         self.mu = np.zeros(self.n_out)
         self.sd = np.ones(self.n_out)
+        self.residual_scatter = None   # per-output training-residual scatter (dex), set by fit()
         self._graphs = {}
 
     # ---- data
@@ -252,7 +268,22 @@ class Emulator:
             if log is not None and (ep % max(1, epochs // 10) == 0 or ep == epochs - 1):
                 log(f"epoch {ep}: loss {history[-1]:.5f}")
         self.net.check_status()
+        self.residual_scatter = self._training_residual_scatter(x_all, y)
         return history
+
+    def _training_residual_scatter(self, x_all, y, chunk=4096):
+        """Per output (n_out,), in dex: the standard deviation over the training samples of the
+        ensemble mean's residual, i.e. the emulator's typical error on its own library (the
+        realization noise of the library's statistics plus the fit's error, whose heavy tail makes it
+        larger than the noise alone).  :meth:`predict` can scale each output's spread by it."""
+        t = D.torch()
+        res = []
+        for i0 in range(0, x_all.shape[0], chunk):
+            out = self.net.forward(x_all[i0:i0 + chunk].contiguous())
+            res.append(D.to_host(out.mean(dim=0))[:, :self.n_out].astype(np.float64))
+        self.net.check_status()
+        pred = np.concatenate(res) * self.sd + self.mu
+        return np.std(pred - y, axis=0)
 
     # ---- queries
 
@@ -263,24 +294,38 @@ class Emulator:
         out = out * self.sd + self.mu
         return out.reshape(out.shape[0], out.shape[1], self.nfreqs, 4)
 
-    def predict(self, params, spread_stats=None):
+    def predict(self, params, spread_stats=None, residual_scaled=False, max_spread=0.05):
         """(mean (Q, F, 4), spread (Q,), inside (Q,)): the ensemble mean, the largest standard
         deviation over members (dex) of the statistics named in ``spread_stats`` (default: all of
-        :data:`STATS`) at any frequency, and whether the query lies in the training box."""
+        :data:`STATS`) at any frequency, and whether the query lies in the training box.
+
+        ``residual_scaled``: each output's standard deviation is first divided by its threshold
+        max(``max_spread``, the output's training-residual scatter, see :meth:`fit`) and the largest
+        ratio times ``max_spread`` is returned, so that ``spread > max_spread`` flags a query whose
+        members disagree by more than both ``max_spread`` and the emulator's typical error on that
+        output over its training library."""
         mem = self.predict_members(params)
         u = self.unit(params)
         inside = np.all((u >= 0.0) & (u <= 1.0), axis=1)
         cols = list(range(4)) if spread_stats is None else [STATS.index(nm) for nm in spread_stats]
-        return mem.mean(axis=0), mem.std(axis=0)[..., cols].max(axis=(1, 2)), inside
+        std = mem.std(axis=0)
+        if residual_scaled:
+            if getattr(self, "residual_scatter", None) is None:
+                raise ValueError("residual_scaled needs the residual scatter that fit() records")
+            thr = np.maximum(max_spread, self.residual_scatter.reshape(self.nfreqs, 4))
+            std = std / thr[None] * max_spread
+        return mem.mean(axis=0), std[..., cols].max(axis=(1, 2)), inside
 
-    def query(self, params, fallback=None, max_spread=0.05, spread_stats=None):
+    def query(self, params, fallback=None, max_spread=0.05, spread_stats=None, residual_scaled=False):
         """Statistics (Q, F, 4) with the plain SAM as fallback: queries outside the training box or
-        with ensemble spread (of ``spread_stats``, see :meth:`predict`) above ``max_spread`` dex are
-        re-solved by ``fallback(param_row) -> (F, 4)`` (e.g. :func:`sam_fallback`).  Returns (stats,
-        solved_by_sam mask).  If the network's kernels fail (a tensor-core wait gave up), every query
-        is re-solved by ``fallback``; without one the error is raised."""
+        with ensemble spread (of ``spread_stats``, optionally residual-scaled, see :meth:`predict`)
+        above ``max_spread`` dex are re-solved by ``fallback(param_row) -> (F, 4)`` (e.g.
+        :func:`sam_fallback`).  Returns (stats, solved_by_sam mask).  If the network's kernels fail
+        (a tensor-core wait gave up), every query is re-solved by ``fallback``; without one the
+        error is raised."""
         try:
-            mean, spread, inside = self.predict(params, spread_stats=spread_stats)
+            mean, spread, inside = self.predict(params, spread_stats=spread_stats, residual_scaled=residual_scaled,
+                                                max_spread=max_spread)
             redo = (~inside) | (spread > max_spread)
         except N.NativeError:
             if fallback is None:
@@ -293,28 +338,36 @@ class Emulator:
                 mean[qq] = fallback(np.atleast_2d(params)[qq])
         return mean, redo
 
-    def graphed(self, batch):
+    def graphed(self, batch, fused=None):
         """A CUDA-graph query path for batches of ``batch`` parameter rows: the host-to-device copy of
-        the inputs, every layer's kernel and the device-to-host copy of the outputs replay as one
-        graph launch.  Returns a callable params (Q <= batch, P) -> ensemble-mean statistics (Q, F, 4)."""
-        g = self._graphs.get(batch)
+        the inputs, the network (the fused one-launch forward up to ``_native.MLP_FUSED_MAX_BATCH``
+        rows, the tensor-core layers above) and the device-to-host copy of the outputs replay as one
+        graph launch.  Returns a callable params (Q <= batch, P) -> ensemble-mean statistics (Q, F, 4).
+        ``fused``: force (True) or exclude (False) the fused forward; None picks by batch."""
+        use_fused = (batch <= N.MLP_FUSED_MAX_BATCH) if fused is None else bool(fused)
+        key = (int(batch), use_fused)
+        g = self._graphs.get(key)
         if g is None:
-            g = _GraphedForward(self, batch)
-            self._graphs[batch] = g
+            g = _GraphedForward(self, batch, use_fused)
+            self._graphs[key] = g
         return g
 
     def state(self):
+        rs = getattr(self, "residual_scatter", None)
+        extra = {} if rs is None else dict(residual_scatter=rs)
         return dict(lo=self.lo, hi=self.hi, mu=self.mu, sd=self.sd, nfreqs=self.nfreqs,
-                    param_names=np.array(self.param_names), **self.net.state())
+                    param_names=np.array(self.param_names), **extra, **self.net.state())
 
     def load_state(self, state):
         self.mu = np.asarray(state["mu"], dtype=np.float64)
         self.sd = np.asarray(state["sd"], dtype=np.float64)
+        self.residual_scatter = (np.asarray(state["residual_scatter"], dtype=np.float64)
+                                 if "residual_scatter" in state else None)
         self.net.load_params(state["params"])
 
 
 class _GraphedForward:
-    def __init__(self, emu, batch):
+    def __init__(self, emu, batch, fused):
         t = D.torch()
         self.emu = emu
         self.batch = int(batch)
@@ -327,18 +380,38 @@ class _GraphedForward:
         # the kernels' status word travels back with the outputs; it is cleared at the start of each
         # replay, so every call reports only its own kernels
         self.h_status = t.zeros(1, dtype=t.int32).pin_memory()
+        self.h_status_np = self.h_status.numpy()
         self.stream = t.cuda.Stream(device=dev)
+        self.fused = bool(fused)
+        if self.fused and self.batch > N.MLP_FUSED_MAX_BATCH:
+            raise ValueError(f"the fused forward takes at most {N.MLP_FUSED_MAX_BATCH} rows")
         with t.cuda.stream(self.stream):
-            emu.net.forward(self.d_in, owner=self)   # eager pass: lazy kernel attributes, this graph's buffers
-            self.stream.synchronize()
-            emu.net.check_status()
-            self.graph = t.cuda.CUDAGraph()
-            with t.cuda.graph(self.graph, stream=self.stream):
-                emu.net.status.t.zero_()
-                self.d_in.copy_(self.h_in, non_blocking=True)
-                out = emu.net.forward(self.d_in, owner=self)
-                self.h_out.copy_(out, non_blocking=True)
-                self.h_status.copy_(emu.net.status.t, non_blocking=True)
+            if self.fused:
+                # one kernel node: it reads the pinned inputs and writes the pinned outputs and status
+                # word itself (device-accessible host memory), so the graph has no copy nodes
+                net = emu.net
+
+                def launch():
+                    N.call("hgb_mlp_forward_fused", ctypes.byref(net.struct), N.ptr(self.h_in), 0, self.batch,
+                           N.ptr(self.h_out), N.ptr(self.h_status), N.stream_handle())
+
+                launch()   # eager pass: the kernel's shared-memory attribute is set outside the capture
+                self.stream.synchronize()
+                net.check_status(int(self.h_status_np[0]))
+                self.graph = t.cuda.CUDAGraph()
+                with t.cuda.graph(self.graph, stream=self.stream):
+                    launch()
+            else:
+                emu.net.forward(self.d_in, owner=self)   # eager pass: kernel attributes, this graph's buffers
+                self.stream.synchronize()
+                emu.net.check_status()
+                self.graph = t.cuda.CUDAGraph()
+                with t.cuda.graph(self.graph, stream=self.stream):
+                    emu.net.status.t.zero_()
+                    self.d_in.copy_(self.h_in, non_blocking=True)
+                    out = emu.net.forward(self.d_in, owner=self)
+                    self.h_out.copy_(out, non_blocking=True)
+                    self.h_status.copy_(emu.net.status.t, non_blocking=True)
         self.stream.synchronize()
 
     def __call__(self, params):
@@ -348,12 +421,14 @@ class _GraphedForward:
         if q > self.batch:
             raise ValueError(f"at most {self.batch} queries per call")
         self.h_in_bits[:q, :npar] = bf16_bits(2.0 * u - 1.0).view(np.int16)
+        if self.fused:
+            self.h_status_np[0] = 0   # the kernel only sets bits
         with t.cuda.stream(self.stream):
             self.graph.replay()
         self.stream.synchronize()
-        self.emu.net.check_status(int(self.h_status[0]))
-        out = self.h_out_np[:, :q, :self.emu.n_out].astype(np.float64) * self.emu.sd + self.emu.mu
-        return out.mean(axis=0).reshape(q, self.emu.nfreqs, 4)
+        self.emu.net.check_status(int(self.h_status_np[0]))
+        out = self.h_out_np[:, :q, :self.emu.n_out].mean(axis=0, dtype=np.float64) * self.emu.sd + self.emu.mu
+        return out.reshape(q, self.emu.nfreqs, 4)
 
 
 def sample_statistics(res):
@@ -379,15 +454,16 @@ def training_library(space, sam_shape=(91, 81, 101), nreals=500, nfreqs=40, seed
     return library_statistics(res)
 
 
-def sam_fallback(space, sam_shape=(91, 81, 101), nreals=500, nfreqs=40, nloudest=1, seed=0):
-    """fallback(param_row) -> (F, 4): the plain GPU SAM at those parameters."""
+def sam_fallback(space, sam_shape=(91, 81, 101), nreals=500, nfreqs=40, nloudest=1, seed=0, precision="fp64"):
+    """fallback(param_row) -> (F, 4): the plain GPU SAM at those parameters (grid arithmetic in
+    ``precision``, see :meth:`Semi_Analytic_Model.gwb`)."""
     from .librarian import lib_tools
 
     def solve(row):
         params = dict(zip(space.param_names, np.asarray(row, dtype=np.float64)))
         sam, hard = space.model_for_params(params, sam_shape)
         res = lib_tools.run_model(sam, hard, nfreqs=nfreqs, nreals=nreals, nloudest=nloudest, gwb_flag=False,
-                                  singles_flag=True, seed=seed)
+                                  singles_flag=True, seed=seed, precision=precision)
         return strain_statistics(res["hc_ss"], res["hc_bg"])
 
     return solve

@@ -444,6 +444,17 @@ long hgb_mlp_weight_count(const hgb_mlp *net);   /* Pw, or -1 */
  * pre may be NULL (inference). */
 int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, uint16_t *act,
                     float *pre, float *out, int *d_status, void *stream);
+/* The same outputs as hgb_mlp_forward (out [member][batch][dims[n_layers]]) for batch <=
+ * HGB_MLP_FUSED_MAX_BATCH in ONE launch: a cluster of 8 CTAs per member holds every layer's
+ * weights (bulk-copied into shared memory at the start) and the activations on chip, with the
+ * products on the CUDA cores (fp32 sums, bf16 activations as in hgb_mlp_forward; the summation
+ * order differs).  For query latency; no act / pre buffers.  `weights` must be 16-byte aligned.
+ * x, out and d_status are accessed with plain loads and stores, so they may also be pinned host
+ * memory; d_status's bit is set by a plain read-modify-write (do not share the word with kernels
+ * that run concurrently). */
+#define HGB_MLP_FUSED_MAX_BATCH 16
+int hgb_mlp_forward_fused(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, float *out,
+                          int *d_status, void *stream);
 size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch);
 /* Mean-squared-error loss against target [batch][dims[n_layers]] (target_member_stride apart) of the
  * outputs of the last hgb_mlp_forward (with pre): loss[e] (may be NULL) and grad [E][P] fp32. */

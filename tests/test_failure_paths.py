@@ -82,7 +82,7 @@ def test_emulator_query_falls_back_when_the_network_fails():
     emu = Emulator.__new__(Emulator)
     emu.nfreqs = 3
 
-    def failing_predict(params, spread_stats=None):
+    def failing_predict(params, spread_stats=None, **kwargs):
         raise N.NativeError("an MLP kernel timed out waiting for the tensor core")
 
     emu.predict = failing_predict

@@ -121,6 +121,50 @@ def test_forward_exact_on_small_integers(built_lib, dims, batch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("dims,batch", [([16, 32], 1), ([256, 160], 16), ([64, 48, 32], 5), ([16, 256, 256, 160], 3)])
+def test_fused_forward_exact_on_small_integers(built_lib, dims, batch):
+    """The one-launch fused forward on integer weights, biases and inputs: exact sums, so the outputs
+    equal the oracle bit for bit (weight slices of every cluster rank, activation exchange between
+    the CTAs, ragged query counts)."""
+    import torch
+    rng = np.random.default_rng(len(dims) * 100 + batch)
+    E = 3
+    net = _ensemble(dims, E)
+    layers = [[(rng.integers(-3, 4, size=(n, k)).astype(np.float32), rng.integers(-5, 6, size=n).astype(np.float32))
+               for k, n in zip(dims[:-1], dims[1:])] for _ in range(E)]
+    for m in range(E):   # the SiLU's rounding is not an integer: a zero layer after it keeps sums exact
+        for ll in range(1, len(layers[m])):
+            layers[m][ll] = (np.zeros_like(layers[m][ll][0]), layers[m][ll][1])
+    _set_layers(net, layers)
+    x = rng.integers(-3, 4, size=(batch, dims[0])).astype(np.float32)
+    out = net.forward_fused(_bf16_tensor(x)).cpu().numpy()
+    torch.cuda.synchronize()
+    net.check_status()
+    for m in range(E):
+        _, _, exp = MO.forward(layers[m], x)
+        assert np.array_equal(out[m], exp), m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batch", [1, 7, 16])
+def test_fused_forward_matches_tensor_core_forward(built_lib, batch):
+    """The emulator's network shape with random weights: the fused forward agrees with the tensor-core
+    layers within the bf16 activation rounding (their fp32 sums run in different orders)."""
+    import torch
+    rng = np.random.default_rng(batch)
+    dims = [16, 256, 256, 256, 256, 160]
+    E = 4
+    net = _ensemble(dims, E)
+    _set_layers(net, [_rand_layers(rng, dims) for _ in range(E)])
+    x = _bf16_tensor(rng.uniform(-1, 1, size=(batch, 16)))
+    ref = net.forward(x).cpu().numpy()
+    got = net.forward_fused(x).cpu().numpy()
+    net.check_status()
+    assert got.shape == ref.shape
+    assert np.abs(got - ref).max() <= 1e-2 * np.abs(ref).max(), np.abs(got - ref).max() / np.abs(ref).max()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("k,batch", [(16, 256), (256, 128)])
 def test_weight_gradient_exact_on_small_integers(built_lib, k, batch):
     """One linear layer, targets chosen so that d loss / d out is a small integer: the weight and bias
@@ -247,6 +291,9 @@ def test_emulator_learns_a_library_and_beats_the_baselines(built_lib):
     assert np.median(err) < 0.25 * np.median(err_mean), (np.median(err), np.median(err_mean))
     g = emu.graphed(64)
     assert np.allclose(g(test.param_samples), mean, rtol=0, atol=1e-9)
+    g1 = emu.graphed(1)                                    # the fused one-kernel graph (pinned I/O)
+    for row in test.param_samples[:5]:
+        assert np.allclose(g1(row[None]), emu.predict(row[None])[0], rtol=0, atol=1e-2)
     t_emu = EM.timed(g, test.param_samples, repeat=20) / 64
     solve = EM.sam_fallback(train, sam_shape=shape, nreals=nr, nfreqs=nf, seed=3)
     t_sam = EM.timed(solve, test.param_samples[0], repeat=3)
