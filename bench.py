@@ -480,6 +480,8 @@ def run_emulator(args):
     n_te = max(64, n_tr // 10)
     sp_tr = PS_Classic_Phenom_Uniform(nsamples=n_tr, seed=0)
     sp_te = PS_Classic_Phenom_Uniform(nsamples=n_te, seed=1)
+    n_bd = args.emulator_boundary_samples
+    sp_bd = EM.boundary_space(PS_Classic_Phenom_Uniform, n_bd, seed=2) if n_bd > 0 else None
     lib_stats = {}
     cache = args.emulator_cache
     if cache and os.path.exists(cache):
@@ -487,22 +489,44 @@ def run_emulator(args):
             assert np.array_equal(z["params_train"], sp_tr.param_samples), "cache holds another library"
             y_tr, y_te, y_te2 = z["y_train"], z["y_test"], z["y_test2"]
             lib_stats["seconds"] = float(z["library_seconds"])
+            cached = {kk: z[kk] for kk in z.files}
+        if sp_bd is None:
+            y_bd, bd_seconds = np.zeros((0,) + y_tr.shape[1:]), 0.0
+        elif "y_boundary" in cached and np.array_equal(cached.get("params_boundary"), sp_bd.param_samples):
+            y_bd, bd_seconds = cached["y_boundary"], float(cached["boundary_seconds"])
+        else:
+            bd_stats = {}
+            y_bd = EM.training_library(sp_bd, seed=6, stats=bd_stats, precision=args.precision)
+            bd_seconds = bd_stats["seconds"]
+            np.savez(cache, **dict(cached, params_boundary=sp_bd.param_samples, y_boundary=y_bd,
+                                   boundary_seconds=bd_seconds))
     else:
         y_tr = EM.training_library(sp_tr, seed=2, stats=lib_stats, precision=args.precision)
         y_te = EM.training_library(sp_te, seed=3, precision=args.precision)
         # the first NOISE_SAMPLES held-out models again with other realizations: the noise floor
         y_te2 = EM.training_library(sp_te, seed=4, precision=args.precision,
                                     indices=list(range(min(NOISE_SAMPLES, n_te))))
+        y_bd, bd_seconds, extra = np.zeros((0,) + y_tr.shape[1:]), 0.0, {}
+        if sp_bd is not None:
+            bd_stats = {}
+            y_bd = EM.training_library(sp_bd, seed=6, stats=bd_stats, precision=args.precision)
+            bd_seconds = bd_stats["seconds"]
+            extra = dict(params_boundary=sp_bd.param_samples, y_boundary=y_bd, boundary_seconds=bd_seconds)
         if cache:
             np.savez(cache, params_train=sp_tr.param_samples, params_test=sp_te.param_samples, y_train=y_tr,
-                     y_test=y_te, y_test2=y_te2, library_seconds=lib_stats["seconds"])
+                     y_test=y_te, y_test2=y_te2, library_seconds=lib_stats["seconds"], **extra)
+    # the training set: the Latin hypercube, plus any points on the box's faces
+    x_bd = sp_bd.param_samples if sp_bd is not None else np.zeros((0, sp_tr.param_samples.shape[1]))
+    x_fit = np.concatenate([sp_tr.param_samples, x_bd])
+    y_fit = np.concatenate([y_tr, y_bd])
+    ok_fit = np.all(np.isfinite(y_fit), axis=(1, 2))
     ok = np.all(np.isfinite(y_tr), axis=(1, 2))
     emu = EM.Emulator(sp_tr, nfreqs=NFREQ, members=4, width=256, depth=4, seed=0)
-    steps_per_epoch = max(1, int(ok.sum()) // 512)
+    steps_per_epoch = max(1, int(ok_fit.sum()) // 512)
     epochs = max(50, -(-args.emulator_steps // steps_per_epoch))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    hist = emu.fit(sp_tr.param_samples[ok], y_tr[ok], epochs=epochs, batch=512, lr=2e-3)
+    hist = emu.fit(x_fit[ok_fit], y_fit[ok_fit], epochs=epochs, batch=512, lr=2e-3)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     mean, spread, inside = emu.predict(sp_te.param_samples)
@@ -532,8 +556,10 @@ def run_emulator(args):
     def med(a):
         return {nm: float(np.median(a[..., k])) for k, nm in enumerate(names)}
 
-    return {"workload": EMU_CONFIG, "train_samples": int(ok.sum()), "test_samples": int(good.sum()),
+    return {"workload": EMU_CONFIG, "train_samples": int(ok.sum()), "boundary_samples": int(ok_fit.sum() - ok.sum()),
+            "test_samples": int(good.sum()),
             "library_seconds": lib_stats.get("seconds"), "library_samples_per_s": n_tr / lib_stats["seconds"],
+            "boundary_library_seconds": bd_seconds,
             "train_seconds": t_train, "train_steps": epochs * steps_per_epoch, "final_loss": hist[-1],
             "median_abs_dlog10": med(err), "p95_abs_dlog10": {nm: float(np.percentile(err[..., k], 95))
                                                              for k, nm in enumerate(names)},
@@ -835,7 +861,9 @@ def main():
     ap.add_argument("--batched", action="store_true", help="only the batched-library measurement")
     ap.add_argument("--emulator-samples", type=int, default=20000,
                     help="training samples of the emulator measurement carried by the bench line (0: skip)")
-    ap.add_argument("--emulator-steps", type=int, default=15000, help="emulator training steps (batch 512)")
+    ap.add_argument("--emulator-steps", type=int, default=60000, help="emulator training steps (batch 512)")
+    ap.add_argument("--emulator-boundary-samples", type=int, default=0,
+                    help="training points on the faces of the parameter box, added to the Latin hypercube")
     ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
     ap.add_argument("--mlp-profile", action="store_true", help="untimed emulator-network kernels (for ncu)")
     ap.add_argument("--highres-steps", type=int, default=1,

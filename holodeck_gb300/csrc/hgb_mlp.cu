@@ -669,7 +669,8 @@ const float *param_bias(const hgb_mlp *net, const NetView &v, int l) { return ne
 // copies overlap the first layers' arithmetic) into shared memory.  A layer is a matrix-vector
 // product per query on the CUDA cores (a batch of at most FUSED_QMAX rows would leave a 128-row
 // tensor-core tile almost empty): each warp takes every fourth column, its lanes split the
-// reduction axis in runs of 8, fp32 products and a warp-shuffle sum.  The hidden activations
+// reduction axis in runs of 8, fp32 products, and the warp's columns are summed together by one
+// transposing shuffle reduction.  The hidden activations
 // (bias, SiLU, rounded to bf16 as in the layered forward) are stored into the next activation
 // buffer of every CTA of the cluster (distributed shared memory), and one cluster barrier per layer
 // publishes them; the buffers alternate, so a CTA writing layer l + 1's inputs never meets a peer
@@ -762,23 +763,44 @@ __global__ void __cluster_dims__(FUSED_CL, 1, 1) __launch_bounds__(FUSED_THREADS
         bf16 *Y = (l & 1) ? act0 : act1;
         const float *bias = sbias + l * FUSED_NCMAX;
         const bool last = l == a.L - 1;
-        for (int n = warp; n < nc; n += FUSED_THREADS / 32) {
-            const bf16 *wr = W + (long)n * K;
-            for (int q = 0; q < Q; q++) {
-                float acc = 0.0f;
-                for (int kc = lane; kc < K / 8; kc += 32)
-                    acc = dot8_bf16(*(const uint4 *)(wr + kc * 8), *(const uint4 *)(X + q * WIDTH + kc * 8), acc);
+        // warp w: columns n = w + 4 j, j < ncw (at most 8); lane k: reduction entries 8k .. 8k + 7
+        // (K <= 256, so one run per lane).  The eight column sums are reduced together: three
+        // exchange levels halve the set a lane carries (4 + 2 + 1 shuffles), two more finish the
+        // sum, and lane 4 j ends with column j's total, so the eight epilogues run side by side.
+        const int ncw = (nc - warp + 3) / 4;
+        const bool has_run = lane < K / 8;
+        const int jl = 4 * ((lane >> 4) & 1) + 2 * ((lane >> 3) & 1) + ((lane >> 2) & 1);
+        for (int q = 0; q < Q; q++) {
+            float v[8];
+            const uint4 xv = has_run ? *(const uint4 *)(X + q * WIDTH + lane * 8) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0) {
-                    const float z = acc + bias[n];
-                    if (last) {
-                        a.out[((long)e * Q + q) * N + c0 + n] = z;
-                    } else {
-                        const bf16 y = __float2bfloat16_rn(silu(z));
+            for (int j = 0; j < 8; j++)
+                v[j] = (has_run && j < ncw) ? dot8_bf16(*(const uint4 *)(W + (long)(warp + 4 * j) * K + lane * 8), xv, 0.0f)
+                                            : 0.0f;
+            const bool h1 = (lane >> 4) & 1, h2 = (lane >> 3) & 1, h3 = (lane >> 2) & 1;
+            float w4[4], w2[2];
 #pragma unroll
-                        for (int r = 0; r < FUSED_CL; r++) cluster.map_shared_rank(Y, r)[q * WIDTH + c0 + n] = y;
-                    }
+            for (int i = 0; i < 4; i++) {
+                const float keep = h1 ? v[i + 4] : v[i], give = h1 ? v[i] : v[i + 4];
+                w4[i] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const float keep = h2 ? w4[i + 2] : w4[i], give = h2 ? w4[i] : w4[i + 2];
+                w2[i] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+            }
+            float acc = (h3 ? w2[1] : w2[0]) + __shfl_xor_sync(0xffffffffu, h3 ? w2[0] : w2[1], 4);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            if ((lane & 3) == 0 && jl < ncw) {
+                const int n = warp + 4 * jl;
+                const float z = acc + bias[n];
+                if (last) {
+                    a.out[((long)e * Q + q) * N + c0 + n] = z;
+                } else {
+                    const bf16 y = __float2bfloat16_rn(silu(z));
+#pragma unroll
+                    for (int r = 0; r < FUSED_CL; r++) cluster.map_shared_rank(Y, r)[q * WIDTH + c0 + n] = y;
                 }
             }
         }

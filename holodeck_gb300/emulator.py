@@ -423,9 +423,9 @@ class _GraphedForward:
         self.h_in_bits[:q, :npar] = bf16_bits(2.0 * u - 1.0).view(np.int16)
         if self.fused:
             self.h_status_np[0] = 0   # the kernel only sets bits
-        with t.cuda.stream(self.stream):
-            self.graph.replay()
-        self.stream.synchronize()
+        cur = t.cuda.current_stream(self.emu.net.device)
+        self.graph.replay()           # on the caller's current stream (a graph replays on any stream)
+        cur.synchronize()
         self.emu.net.check_status(int(self.h_status_np[0]))
         out = self.h_out_np[:, :q, :self.emu.n_out].mean(axis=0, dtype=np.float64) * self.emu.sd + self.emu.mu
         return out.reshape(q, self.emu.nfreqs, 4)
@@ -452,6 +452,23 @@ def training_library(space, sam_shape=(91, 81, 101), nreals=500, nfreqs=40, seed
     res = batch.run_library(space, shapes=sam_shape, nreals=nreals, nfreqs=nfreqs, nloudest=1, seed=seed,
                             reduce=sample_statistics, stats=stats, **kwargs)
     return library_statistics(res)
+
+
+def boundary_space(space_cls, nsamples, seed=0):
+    """A parameter space of ``nsamples`` points on the faces of ``space_cls``'s box: a Latin-hypercube
+    draw (``seed``) with one coordinate per point, chosen uniformly, moved to its lower or upper
+    bound.  A Latin hypercube rarely comes near the faces, so without such points the ensemble
+    extrapolates there and its members disagree; added to a training library they put the faces
+    inside the data.  (Two of the classic space's faces are physical limits, scatter = 0 and the
+    shortest hardening time, so the box itself cannot be widened.)"""
+    sp = space_cls(nsamples=nsamples, seed=seed)
+    rng = np.random.default_rng([int(seed), 1])
+    u = np.array(sp._uniform_samples, dtype=np.float64)
+    k = rng.integers(0, u.shape[1], size=nsamples)
+    u[np.arange(nsamples), k] = rng.integers(0, 2, size=nsamples).astype(np.float64)
+    sp._uniform_samples = u
+    sp.param_samples = np.stack([dist(u[:, ii]) for ii, dist in enumerate(sp._parameters)], axis=1)
+    return sp
 
 
 def sam_fallback(space, sam_shape=(91, 81, 101), nreals=500, nfreqs=40, nloudest=1, seed=0, precision="fp64"):
