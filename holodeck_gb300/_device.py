@@ -4,6 +4,7 @@ PyTorch supplies device memory and streams; all arithmetic runs in the CUDA kern
 ``_build/libholodeck_gb300.so``.
 """
 
+import contextlib
 import ctypes
 
 import numpy as np
@@ -163,6 +164,22 @@ def side_stream(role, dev=None):
     if s is None:
         s = _SIDE_STREAMS.setdefault(key, t.cuda.Stream(device=cur.device))
     return s
+
+
+@contextlib.contextmanager
+def nvtx(name):
+    """An NVTX range named ``name`` around a stage (Nsight Systems timelines, ``ncu --nvtx``
+    filters); a no-op where torch has no NVTX support."""
+    try:
+        torch().cuda.nvtx.range_push(name)
+        pushed = True
+    except Exception:   # no NVTX in this torch build
+        pushed = False
+    try:
+        yield
+    finally:
+        if pushed:
+            torch().cuda.nvtx.range_pop()
 
 
 def workspace(nbytes, dev=None):

@@ -12,6 +12,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libholodeck_gb300.so")
+#: the same library built with -DHGB_BOUNDS_CHECK (holodeck_gb300.build.build(checked=True)); loaded
+#: instead of LIB_PATH when HOLODECK_GB300_CHECKED=1 is set in the environment
+CHECKED_LIB_PATH = os.path.join(_HERE, "_build_checked", "libholodeck_gb300.so")
 
 HGB_OK = 0
 HGB_ERR_INVALID_ARGUMENT = 1
@@ -23,6 +26,7 @@ STATUS_ITERATION_LIMIT = 1
 STATUS_INVALID_REDSHIFT = 2
 STATUS_TABLE_RANGE = 4
 STATUS_GRADIENT_NOT_CONVERGED = 8
+STATUS_BOUNDS = 16
 
 RNG_PHILOX = 0
 RNG_REPLAY = 1
@@ -166,7 +170,8 @@ def load(path=None):
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = path or LIB_PATH
+    if path is None:
+        path = CHECKED_LIB_PATH if os.environ.get("HOLODECK_GB300_CHECKED") == "1" else LIB_PATH
     if not os.path.exists(path):
         raise NativeUnavailable(
             f"holodeck_gb300 CUDA extension not built ({path} missing); run holodeck_gb300.build.build()")
@@ -185,6 +190,12 @@ def exported_symbols():
 
 class NativeError(RuntimeError):
     pass
+
+
+def check_bounds(code, what):
+    """Raise when a bounds-checked build flagged an index outside its array (HGB_STATUS_BOUNDS)."""
+    if code & STATUS_BOUNDS:
+        raise NativeError(f"{what}: an index left its array (device status HGB_STATUS_BOUNDS)")
 
 
 def check(rc, what):

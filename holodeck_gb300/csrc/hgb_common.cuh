@@ -32,6 +32,19 @@ __device__ __forceinline__ void flag(int *d_status, int bits) {
     if (d_status) atomicOr(d_status, bits);
 }
 
+// Compile-time-switchable bounds checks: in a library built with -DHGB_BOUNDS_CHECK,
+// HGB_IN_BOUNDS(cond, status) flags HGB_STATUS_BOUNDS when cond is false and yields cond, so the
+// caller skips (or clamps) the access; otherwise it is the constant true and costs nothing.
+__device__ __forceinline__ bool in_bounds(bool ok, int *d_status) {
+    if (!ok) flag(d_status, HGB_STATUS_BOUNDS);
+    return ok;
+}
+#ifdef HGB_BOUNDS_CHECK
+#define HGB_IN_BOUNDS(cond, status) (hgb::in_bounds((cond), (status)))
+#else
+#define HGB_IN_BOUNDS(cond, status) (true)
+#endif
+
 // Derived constants of the Cython kernels (sam_cyutils.pyx:38-42), evaluated once on the host
 // with the host C library in the same operation order as the Cython module initialisation.
 struct CyConst {

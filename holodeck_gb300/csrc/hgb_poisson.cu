@@ -478,7 +478,8 @@ constexpr int GR = 8;    // thread rows (GT x GR threads, GT / GR rows each)
 __global__ void __launch_bounds__(GT * GR) k_gather_sorted(const double *__restrict__ number,
                                                            const double *__restrict__ h2fdf,
                                                            const int32_t *__restrict__ order, long nb, int nf,
-                                                           double *__restrict__ lam_s, double *__restrict__ h_s) {
+                                                           double *__restrict__ lam_s, double *__restrict__ h_s,
+                                                           int *d_status) {
     __shared__ double tl[GT][GT + 1], th[GT][GT + 1];
     const long k0 = (long)blockIdx.x * GT;
     const int f0 = blockIdx.y * GT;
@@ -488,9 +489,11 @@ __global__ void __launch_bounds__(GT * GR) k_gather_sorted(const double *__restr
         const long k = k0 + j;
         const int f = f0 + tx;
         if (k < nb && f < nf) {
-            const long src = (long)order[k] * nf + f;
-            tl[j][tx] = number[src];
-            th[j][tx] = h2fdf[src];
+            const long o = order[k];
+            const long src = o * nf + f;
+            const bool ok = HGB_IN_BOUNDS(o >= 0 && o < nb, d_status);   // a caller's order
+            tl[j][tx] = ok ? number[src] : 0.0;
+            th[j][tx] = ok ? h2fdf[src] : 0.0;
         }
     }
     __syncthreads();
@@ -506,9 +509,9 @@ __global__ void __launch_bounds__(GT * GR) k_gather_sorted(const double *__restr
 }
 
 void launch_gather_sorted(const double *number, const double *h2fdf, const int32_t *order, long nb, int nf,
-                          double *lam_s, double *h_s, cudaStream_t st) {
+                          double *lam_s, double *h_s, cudaStream_t st, int *d_status) {
     dim3 grid((unsigned)hgb::ceil_div(nb, GT), (unsigned)hgb::ceil_div(nf, GT));
-    k_gather_sorted<<<grid, dim3(GT, GR), 0, st>>>(number, h2fdf, order, nb, nf, lam_s, h_s);
+    k_gather_sorted<<<grid, dim3(GT, GR), 0, st>>>(number, h2fdf, order, nb, nf, lam_s, h_s, d_status);
 }
 
 // ---- 2. cumulative expectation along the sorted bins: C[0] = 0, C[k + 1] = C[k] + max(lambda_k, 0)
@@ -686,6 +689,7 @@ __global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict
             else lo = mid + 1;
         }
         const long j = lo;
+        if (!HGB_IN_BOUNDS(j >= i && j < nb, d_status)) break;
         const double lj = lam[j];
         double num;
         if (lj > NORMAL_THRESH) {
@@ -706,7 +710,8 @@ __global__ void k_loud_prefix(PrefixArgs a, ParArgs pa, const double *__restrict
         if (num < 1.0) continue;   // cyutils.pyx:1331-1332
         const double cur = h[j];
         if (PARAMS && cur == 0.0) continue;   // cyutils.pyx:1710 (not reached: such bins are masked in C)
-        const long bin = PARAMS ? (long)pa.order[j] : 0;
+        long bin = PARAMS ? (long)pa.order[j] : 0;
+        if (!HGB_IN_BOUNDS(bin >= 0 && bin < nb, d_status)) bin = 0;
         while (nfill < a.nl && num > 0.0) {   // cyutils.pyx:1336-1340, 1711-1723
             ss[nfill] = cur;
             if (PARAMS) {
@@ -1144,7 +1149,9 @@ __device__ __forceinline__ void bulk_block(const BulkArgs &a, const ParArgs &pa,
                             const uint32_t uc = min(u, 0xFFFFFFFEu);   // below cdf[S - 1]
                             const unsigned g = guide[uc >> shift];
                             int e = (int)(g & GUIDE_M);
+                            if (!HGB_IN_BOUNDS(e < S - 1 || !(g & GUIDE_ONE), d_status)) e = 0;
                             if (g & GUIDE_ONE) e += (uc >= cdf[e]) ? 1 : 0;
+                            if (!HGB_IN_BOUNDS(e < S, d_status)) e = S - 1;
                             const bool tail = !(g & (GUIDE_PURE | GUIDE_ONE));
                             pend |= tail ? (1u << sl) : 0u;
                             if (!tail && (!check || pos >= __ldg(q_row + sl * RB))) {
@@ -1167,6 +1174,7 @@ __device__ __forceinline__ void bulk_block(const BulkArgs &a, const ParArgs &pa,
                             const unsigned cell = uc >> shift;
                             int lo = (int)(guide[cell] & GUIDE_M);
                             int hi = (cell + 1 < (1u << gb)) ? (int)(guide[cell + 1] & GUIDE_M) : S - 1;
+                            if (!HGB_IN_BOUNDS(lo <= hi && hi < S, d_status)) lo = hi = S - 1;
                             while (lo < hi) {   // cdf[hi] > uc throughout
                                 const int mid = (lo + hi) >> 1;
                                 if (uc >= cdf[mid]) lo = mid + 1;
@@ -1381,9 +1389,10 @@ __device__ __forceinline__ void bulk_block(const BulkArgs &a, const ParArgs &pa,
             }
         }
     }
+    const bool part_ok = HGB_IN_BOUNDS(c < a.nchunk && f < a.nf, d_status);
 #pragma unroll
     for (int i = 0; i < RPT; i++)
-        if (i < rpt)
+        if (i < rpt && part_ok)
             part[((long)c * a.nf + f) * a.nr + r0 + (long)i * RB] =
                 (((double)acc_r[i] - (double)comp_r[i]) + slot_value(st, i, t)) * HSCALE_INV;
     if (PARAMS) {
@@ -1798,7 +1807,7 @@ int hgb_loudest_hc_from_sorted_ex(const double *number, const double *h2fdf, lon
     double *lam_s = (double *)(w + L.off_lam);
     double *h_s = (double *)(w + L.off_h);
     const long nfr = (long)n_freq * nreals;
-    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st);
+    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st, d_status);
     int rc = hgb::check_launch();
     if (rc) return rc;
     if (mode == HGB_RNG_REPLAY) {
@@ -1890,7 +1899,7 @@ int hgb_loudest_hc_batch(const hgb_loudest_sample *samples, int n_samples, int n
         char *sw = (char *)S.workspace;
         double *lam_s = (double *)(sw + L.off_lam);
         double *h_s = (double *)(sw + L.off_h);
-        launch_gather_sorted(S.number, S.h2fdf, S.order, S.n_bins, n_freq, lam_s, h_s, st);
+        launch_gather_sorted(S.number, S.h2fdf, S.order, S.n_bins, n_freq, lam_s, h_s, st, S.d_status);
         if ((rc = hgb::check_launch())) return rc;
         double *cum = (double *)(sw + L.off_cum);
         int *q = (int *)(sw + L.off_q);
@@ -2021,7 +2030,7 @@ int hgb_loudest_hc_and_par_from_sorted(const double *number, const double *h2fdf
     pa.nq = n_q;
     pa.nz = n_z;
     pa.sspar = sspar;
-    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st);
+    launch_gather_sorted(number, h2fdf, order, n_bins, n_freq, lam_s, h_s, st, d_status);
     int rc = hgb::check_launch();
     if (rc) return rc;
     if (mode == HGB_RNG_REPLAY) {

@@ -263,5 +263,6 @@ def loudest_hc_and_par_from_sorted_redz(number, h2fdf, nreals, nloudest, mt, mr,
 
 def _raise_status(st):
     code = st.read()
+    N.check_bounds(code, "realizations")
     if code & N.STATUS_ITERATION_LIMIT:
         raise RuntimeError("a Poisson sampler exhausted its attempt budget (device status ITERATION_LIMIT)")

@@ -43,7 +43,7 @@ class Fixed_Time_2PL_SAM(_Hardening):
         main = t.cuda.current_stream(mt_d.device)
         side = D.side_stream("hardening_norm", mt_d.device)
         side.wait_stream(main)
-        with t.cuda.stream(side):
+        with t.cuda.stream(side), D.nvtx("hgb:hardening_norm"):
             mtot, mrat = t.meshgrid(mt_d, mr_d, indexing="ij")
             shape = tuple(mtot.shape)
             nl, norm = sam_cyutils.find_2pwl_hardening_norm(time, mtot.reshape(-1), mrat.reshape(-1), sepa_init,

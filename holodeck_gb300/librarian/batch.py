@@ -204,16 +204,17 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
                     break
                 res = err = None
                 try:
-                    sam, hard = space.model_for_params(job.params, job.shape)
-                    if batched:
-                        data, _, number, h2fdf = run_model_grids(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs,
-                                                                 nreals=job.nreals, seed=job.seed, **flags)
-                        ev = t.cuda.Event()
-                        ev.record(stream)
-                        ready.put((job, data, number, h2fdf, ev))
-                        continue
-                    res = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
-                                    nloudest=nloudest, seed=job.seed, **flags)
+                    with D.nvtx(f"hgb:sample {job.index}"):
+                        sam, hard = space.model_for_params(job.params, job.shape)
+                        if batched:
+                            data, _, number, h2fdf = run_model_grids(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs,
+                                                                     nreals=job.nreals, seed=job.seed, **flags)
+                            ev = t.cuda.Event()
+                            ev.record(stream)
+                            ready.put((job, data, number, h2fdf, ev))
+                            continue
+                        res = run_model(sam, hard, pta_dur=pta_dur, nfreqs=nfreqs, nreals=job.nreals,
+                                        nloudest=nloudest, seed=job.seed, **flags)
                 except Exception as exc:   # a failed sample gives NaN rows, as in the reference's libraries
                     err = exc
                 finish(job, res, err)

@@ -205,13 +205,14 @@ class Semi_Analytic_Model:
         static_done = t.cuda.Event()
         static_done.record(main)
         side.wait_event(static_done)
-        with t.cuda.stream(side):
+        with t.cuda.stream(side), D.nvtx("hgb:dbn_step_walk"):
             redz_final, diff_num = sam_cyutils.dbn_2pwl_device(fobs_orb, hard, None, mt, mr, rz, gmt_time,
                                                                cosmo=self._cosmo, phase=1)
             walk_done = t.cuda.Event()
             walk_done.record(side)
         gmt_time.record_stream(side)
-        self._scatter_finish(dens, gmt_time, redz_prime)
+        with D.nvtx("hgb:mbulge_scatter"):
+            self._scatter_finish(dens, gmt_time, redz_prime)
         main.wait_event(walk_done)
         redz_final.record_stream(main)
         diff_num.record_stream(main)
@@ -247,14 +248,17 @@ class Semi_Analytic_Model:
         fobs_gw_cents = utils.midpoints(fobs_gw_edges)
         fobs_orb_edges = fobs_gw_edges / 2.0
         fobs_orb_cents = fobs_gw_cents / 2.0
-        redz_final, diff_num = self._dbn_scheduled(hard, fobs_orb_cents, precision=precision)
-        number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final, precision=precision)
-        if params:
-            edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]
-            return single_sources.ss_params_device(edges, redz_final, number, h2fdf, realize, loudest, seed=seed,
-                                                   replay=replay, order=order, cosmo=self._cosmo)
-        return single_sources.ss_realize_device(number, h2fdf, realize, loudest, seed=seed, replay=replay,
-                                                order=order)
+        with D.nvtx("hgb:density_scatter_dbn"):
+            redz_final, diff_num = self._dbn_scheduled(hard, fobs_orb_cents, precision=precision)
+        with D.nvtx("hgb:number_and_strain"):
+            number, h2fdf = self._number_and_strain(fobs_orb_edges, diff_num, redz_final, precision=precision)
+        with D.nvtx("hgb:realizations"):
+            if params:
+                edges = [self.mtot, self.mrat, self.redz, fobs_orb_edges]
+                return single_sources.ss_params_device(edges, redz_final, number, h2fdf, realize, loudest,
+                                                       seed=seed, replay=replay, order=order, cosmo=self._cosmo)
+            return single_sources.ss_realize_device(number, h2fdf, realize, loudest, seed=seed, replay=replay,
+                                                    order=order)
 
     def _number_and_strain(self, fobs_orb_edges, diff_num, redz_final, status=None, precision="fp64"):
         """Device (number, h2fdf) on the (M-1, Q-1, Z-1, F) bins.  With ``status`` the redshift check

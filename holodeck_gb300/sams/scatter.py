@@ -133,6 +133,7 @@ def add_scatter_to_masses_device(mtot, mrat, dens, scatter, refine=4, tol=GRAD_T
     N.call("hgb_add_scatter_to_masses", ctypes.byref(struct), N.ptr(dens), nz, N.ptr(ws), int(ws_bytes), st.ptr,
            N.stream_handle())
     code = st.read()
+    N.check_bounds(code, "M-Mbulge scatter")
     if code & N.STATUS_GRADIENT_NOT_CONVERGED:
         warnings.warn("Gradient estimation did not converge, the results may be inaccurate")
     return dens

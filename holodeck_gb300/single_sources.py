@@ -24,6 +24,7 @@ def sort_order_device(h2fdf):
 
 def check_redshift_status(st):
     code = st.read()
+    N.check_bounds(code, "number and strain")
     if code & N.STATUS_INVALID_REDSHIFT:
         raise ValueError("redz < 0 and !=-1 found in redz, in ss_gws_redz()")
 

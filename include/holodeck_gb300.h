@@ -39,6 +39,8 @@ extern "C" {
 #define HGB_STATUS_INVALID_REDSHIFT 2  /* redz < 0 and != -1 (single_sources.py:95-98) */
 #define HGB_STATUS_TABLE_RANGE 4       /* an interpolation argument left its table */
 #define HGB_STATUS_GRADIENT_NOT_CONVERGED 8  /* scatter gradient solve hit grad_maxiter (scipy only warns) */
+#define HGB_STATUS_BOUNDS 16           /* an index left its array; the access was skipped (only a library
+                                          built with HGB_BOUNDS_CHECK checks, see holodeck_gb300/build.py) */
 
 /* ---- realization modes for hgb_loudest_hc_from_sorted / hgb_sam_poisson_gwb */
 #define HGB_RNG_PHILOX 0   /* counter-based Philox4x32-10 draws keyed by (seed, bin, realization, frequency) */
