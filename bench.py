@@ -521,7 +521,7 @@ def run_emulator(args):
     y_fit = np.concatenate([y_tr, y_bd])
     ok_fit = np.all(np.isfinite(y_fit), axis=(1, 2))
     ok = np.all(np.isfinite(y_tr), axis=(1, 2))
-    emu = EM.Emulator(sp_tr, nfreqs=NFREQ, members=4, width=256, depth=4, seed=0)
+    emu = EM.Emulator(sp_tr, nfreqs=NFREQ, members=args.emulator_members, width=256, depth=4, seed=0)
     steps_per_epoch = max(1, int(ok_fit.sum()) // 512)
     epochs = max(50, -(-args.emulator_steps // steps_per_epoch))
     torch.cuda.synchronize()
@@ -556,7 +556,8 @@ def run_emulator(args):
     def med(a):
         return {nm: float(np.median(a[..., k])) for k, nm in enumerate(names)}
 
-    return {"workload": EMU_CONFIG, "train_samples": int(ok.sum()), "boundary_samples": int(ok_fit.sum() - ok.sum()),
+    return {"workload": EMU_CONFIG.replace("4-member", f"{args.emulator_members}-member"),
+            "train_samples": int(ok.sum()), "boundary_samples": int(ok_fit.sum() - ok.sum()),
             "test_samples": int(good.sum()),
             "library_seconds": lib_stats.get("seconds"), "library_samples_per_s": n_tr / lib_stats["seconds"],
             "boundary_library_seconds": bd_seconds,
@@ -862,6 +863,7 @@ def main():
     ap.add_argument("--emulator-samples", type=int, default=20000,
                     help="training samples of the emulator measurement carried by the bench line (0: skip)")
     ap.add_argument("--emulator-steps", type=int, default=60000, help="emulator training steps (batch 512)")
+    ap.add_argument("--emulator-members", type=int, default=4, help="ensemble members of the emulator")
     ap.add_argument("--emulator-boundary-samples", type=int, default=0,
                     help="training points on the faces of the parameter box, added to the Latin hypercube")
     ap.add_argument("--emulator", action="store_true", help="only the emulator measurement")
