@@ -792,7 +792,8 @@ def run_highres(args):
 def run_mlp_profile(args):
     """The emulator network's kernels at a fixed size, untimed (the program the MLP ncu captures run):
     a 4-member 16 -> 4x256 -> 160 ensemble, one forward of 1024 queries, then one training step
-    (forward, backward, AdamW) on a batch of 512."""
+    (forward, backward, AdamW) on a batch of 512, then the fused forward of single queries
+    (``--warmup`` + 1 launches)."""
     import torch
     from holodeck_gb300.emulator import MLPEnsemble
     net = MLPEnsemble([16, 256, 256, 256, 256, 160], members=4, seed=0)
@@ -802,9 +803,12 @@ def run_mlp_profile(args):
         net.forward(x)
     t = torch.as_tensor(rng.normal(size=(512, 160)).astype(np.float32), device="cuda")
     net.train_step(x[:512].contiguous(), t, lr=1e-3)
+    for _ in range(args.warmup + 1):
+        net.forward_fused(x[:1].contiguous())
     torch.cuda.synchronize()
     net.check_status()
-    print(json.dumps({"profile": "emulator MLP 16-4x256-160, 4 members", "forward_batch": 1024, "train_batch": 512}))
+    print(json.dumps({"profile": "emulator MLP 16-4x256-160, 4 members", "forward_batch": 1024, "train_batch": 512,
+                      "fused_forward_batch": 1}))
 
 
 def run_stages(args):
