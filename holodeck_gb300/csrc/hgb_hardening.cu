@@ -603,11 +603,15 @@ __global__ void k_dbn_gw(CyConst cc, const double *__restrict__ fobs, int NF, co
     }
 }
 
-// The same root, sixteen cells per block (one warp each) in lock step.  The node constants live in
-// registers (node s = lane + 32 k), the trapezoid terms of all sixteen cells go to shared memory,
-// and one warp forms the sixteen ordered sums with one lane per cell, so the step-order summation
-// costs a sixteenth of a warp instruction per step and cell instead of one.  Arithmetic and
-// evaluation sequence are those of warp_lifetime / warp_brent.
+// The same root, one warp per cell and sixteen cells per block.  A lane holds the constants of nodes
+// s = lane + 32 k in registers: the hardening shape, the GW rate and the trapezoid coefficient
+// c[s] = 2 (sepa[s+1] - sepa[s]).  Each Brent round sums the lifetime c[s] / (v[s] + v[s+1]) with
+// one partial per lane and an xor-butterfly reduction.  Every lane ends with the same total
+// (addition is commutative), so the warp's Brent state stays uniform and the warps never wait for
+// one another.  The evaluation sequence is that of warp_brent; only the grouping of the step sum
+// differs from the reference's step order (a relative change of the lifetime near 1e-16, far
+// below the 1e-3 root tolerance, which the root follows unless a Brent comparison falls within
+// that margin: the normalisation is checked against the reference at 1e-10 in log10).
 constexpr int NB_CELLS = 16;
 constexpr int NB_NODES = 10;   // nodes per lane: nsteps + 1 <= 320
 
@@ -616,99 +620,78 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
                                                                        const double *__restrict__ mrat, int n,
                                                                        double *__restrict__ norm_log10,
                                                                        double *__restrict__ norm, int *d_status) {
-    extern __shared__ double smem[];
-    __shared__ double s_time[NB_CELLS];
-    __shared__ int s_active[NB_CELLS];
+    extern __shared__ double smem[];   // [NB_CELLS][S + 1]: each warp's log10 separations
     const int S = a.nsteps;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cell = blockIdx.x * NB_CELLS + warp;
-    const bool valid = cell < n;
-    double *dts = smem;                                  // [NB_CELLS][S]
-    double *crow = smem + (size_t)NB_CELLS * S;          // [NB_CELLS][S + 1]: log10 separations, then c[s]
-    double *myc = crow + (size_t)warp * (S + 1);
-    double *mydt = dts + (size_t)warp * S;
-    const double mt = valid ? mtot[cell] : 1.0, mr = valid ? mrat[cell] : 1.0;
+    if (cell >= n) return;   // the whole warp: no block-wide barrier follows
+    double *row = smem + (size_t)warp * (S + 1);
+    const double mt = mtot[cell], mr = mrat[cell];
     const double mt3 = pow(mt, 3.0), mr12 = pow(1.0 + mr, 2.0);
-    // log10 separation nodes by repeated subtraction (sam_cyutils.pyx:367-383), one lane per cell
-    if (warp == 0 && lane < NB_CELLS) {
-        const int c = blockIdx.x * NB_CELLS + lane;
-        if (c < n) {
-            double *row = crow + (size_t)lane * (S + 1);
-            const double risco_log10 = log10(3.0 * HGB_CY_SCHW * mtot[c]);
-            const double dx = (a.sepa_init_log10 - risco_log10) / S;
-            double sl = a.sepa_init_log10;
-            row[0] = sl;
-            for (int s = 1; s <= S; s++) {
-                sl -= dx;
-                row[s] = sl;
-            }
+    // log10 separation nodes by repeated subtraction (sam_cyutils.pyx:367-383)
+    if (lane == 0) {
+        const double risco_log10 = log10(3.0 * HGB_CY_SCHW * mt);
+        const double dx = (a.sepa_init_log10 - risco_log10) / S;
+        double sl = a.sepa_init_log10;
+        row[0] = sl;
+        for (int s = 1; s <= S; s++) {
+            sl -= dx;
+            row[s] = sl;
         }
     }
-    __syncthreads();
+    __syncwarp();
     // per node: the hardening shape (1 + x)^(gi - go) / x^(gi - 1) and the GW rate, which do not
     // depend on the normalisation, so each Brent round costs one product and one sum per node
-    double rr[NB_NODES], gw[NB_NODES], sp[NB_NODES];
+    double rr[NB_NODES], gw[NB_NODES], sp[NB_NODES], cf[NB_NODES];
 #pragma unroll
     for (int k = 0; k < NB_NODES; k++) {
         const int s = lane + 32 * k;
         rr[k] = 1.0;
         gw[k] = sp[k] = 0.0;
-        if (valid && s <= S) {
-            const double x = pow(10.0, myc[s]);
+        if (s <= S) {
+            const double x = pow(10.0, row[s]);
             const double xx = x / a.rchar;
             rr[k] = pow_ratio_planned(1.0 + xx, -a.go + a.gi, a.p_outer, xx, a.gi - 1.0, a.p_inner);
             gw[k] = cc.c_dadt * mt3 * mr / (x * x * x) / mr12;
             sp[k] = x;
         }
     }
-    __syncwarp();
-    // c[s] = 2 (sepa[s+1] - sepa[s]), s < S (overwrites this warp's log10 row)
+    // c[s] = 2 (sepa[s+1] - sepa[s]) for s < S, 0 beyond
 #pragma unroll
     for (int k = 0; k < NB_NODES; k++) {
         double nxt = __shfl_down_sync(0xffffffffu, sp[k], 1);
         const double wrap = __shfl_sync(0xffffffffu, (k + 1 < NB_NODES) ? sp[k + 1] : 0.0, 0);
         if (lane == 31) nxt = wrap;
         const int s = lane + 32 * k;
-        if (valid && s < S) myc[s] = 2.0 * (nxt - sp[k]);
+        cf[k] = (s < S) ? 2.0 * (nxt - sp[k]) : 0.0;
     }
-    __syncthreads();
 
-    // Brent's method as in warp_brent, one evaluation per round for every unfinished cell
+    // Brent's method as in warp_brent, one evaluation per round
     double xa = NORM_LOG10_LO, xb = NORM_LOG10_HI, xc = 0.0, fa = 0.0, fb = 0.0, fc = 0.0, d = 0.0, e = 0.0;
     int stage = 0, it = 0, nit = 0;
-    bool done = !valid;
     double root = 0.0;
     for (int round = 0; round < BRENT_MAXITER + 2; round++) {
         const double xe = (stage == 0) ? xa : xb;
-        if (!done) {
-            const double nrm = pow(10.0, xe);
-            double v[NB_NODES];
+        const double nrm = pow(10.0, xe);
+        double v[NB_NODES];
 #pragma unroll
-            for (int k = 0; k < NB_NODES; k++) {
-                double dl = -nrm * rr[k];
-                dl += gw[k];
-                v[k] = dl;
-            }
+        for (int k = 0; k < NB_NODES; k++) {
+            double dl = -nrm * rr[k];
+            dl += gw[k];
+            v[k] = dl;
+        }
+        double part = 0.0;
 #pragma unroll
-            for (int k = 0; k < NB_NODES; k++) {
-                double vn = __shfl_down_sync(0xffffffffu, v[k], 1);
-                const double wrap = __shfl_sync(0xffffffffu, (k + 1 < NB_NODES) ? v[k + 1] : 0.0, 0);
-                if (lane == 31) vn = wrap;
-                const int s = lane + 32 * k;
-                if (s < S) mydt[s] = myc[s] / (v[k] + vn);
-            }
+        for (int k = 0; k < NB_NODES; k++) {
+            double vn = __shfl_down_sync(0xffffffffu, v[k], 1);
+            const double wrap = __shfl_sync(0xffffffffu, (k + 1 < NB_NODES) ? v[k + 1] : 0.0, 0);
+            if (lane == 31) vn = wrap;
+            const int s = lane + 32 * k;
+            if (s < S) part += cf[k] / (v[k] + vn);
         }
-        if (lane == 0) s_active[warp] = done ? 0 : 1;
-        __syncthreads();
-        if (warp == 0 && lane < NB_CELLS && s_active[lane]) {
-            const double *row = dts + (size_t)lane * S;
-            double time = 0.0;
-            for (int s = 0; s < S; s++) time += row[s];
-            s_time[lane] = time;
-        }
-        __syncthreads();
-        if (done) continue;
-        const double fv = s_time[warp] - a.target_time;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        const double fv = part - a.target_time;
         if (stage == 0) {
             fa = fv;
             stage = 1;
@@ -719,18 +702,15 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
             stage = 2;
             if (fa * fb > 0.0) {
                 root = 0.0;
-                done = true;
-                continue;
+                break;
             }
             if (fa == 0.0) {
                 root = xa;
-                done = true;
-                continue;
+                break;
             }
             if (fb == 0.0) {
                 root = xb;
-                done = true;
-                continue;
+                break;
             }
             xc = xa;
             fc = fa;
@@ -742,8 +722,7 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
             if (it >= BRENT_MAXITER) {
                 root = xb;
                 nit = BRENT_MAXITER + 1;
-                done = true;
-                continue;
+                break;
             }
         }
         nit = it + 1;
@@ -761,8 +740,7 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
         const double m = 0.5 * (xc - xb);
         if (fb == 0.0 || fabs(m) < tol) {
             root = xb;
-            done = true;
-            continue;
+            break;
         }
         if (fabs(e) > tol && fabs(fb) < fabs(fa)) {
             double sst;
@@ -788,14 +766,14 @@ __global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst
         fa = fb;
         xb = xb + ((fabs(d) > tol) ? d : ((m > 0.0) ? tol : -tol));
     }
-    if (valid && lane == 0) {
+    if (lane == 0) {
         norm_log10[cell] = root;
         if (norm) norm[cell] = pow(10.0, root);
         if (nit > BRENT_MAXITER) hgb::flag(d_status, HGB_STATUS_ITERATION_LIMIT);
     }
 }
 
-size_t norm_blk_smem(int nsteps) { return sizeof(double) * (size_t)NB_CELLS * (2 * (size_t)nsteps + 1); }
+size_t norm_blk_smem(int nsteps) { return sizeof(double) * (size_t)NB_CELLS * ((size_t)nsteps + 1); }
 
 size_t norm_smem_per_warp(int nsteps) { return (size_t)5 * (nsteps + 1) * sizeof(double); }
 
