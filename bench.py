@@ -546,7 +546,8 @@ def run_emulator(args):
     g1, gb = emu.graphed(1), emu.graphed(1024)
     q1 = sp_te.param_samples[:1]
     qb = np.resize(sp_te.param_samples, (1024, sp_te.param_samples.shape[1]))
-    t_q1 = EM.timed(g1, q1, repeat=200)
+    t_q1_graph = EM.timed(g1, q1, repeat=200)
+    t_q1 = EM.timed(emu.native(1), q1, repeat=500)
     t_q1_tc = EM.timed(emu.graphed(1, fused=False), q1, repeat=200)
     # the fused kernel alone: 200 launches back to back between CUDA events (weights L2-resident)
     x1 = emu.inputs(q1)
@@ -583,7 +584,10 @@ def run_emulator(args):
             "accepted_median_abs_dlog10_by_criterion": {
                 nm: med(np.abs(mean - y_te)[good & (sv <= 0.05)]) for nm, sv in criteria},
             "training_residual_scatter_median_dex": float(np.median(emu.residual_scatter)),
-            "query_s_batch1": t_q1, "query_s_batch1_tensor_core_layers": t_q1_tc,
+            "query_s_batch1": t_q1, "query_s_batch1_paths": {
+                "native (one hgb_emulator_query call)": t_q1, "graph, fused kernel, pinned I/O": t_q1_graph,
+                "graph, tensor-core layers and copy nodes": t_q1_tc},
+            "query_s_batch1_tensor_core_layers": t_q1_tc,
             "fused_kernel_s_back_to_back": t_fused_kernel,
             "query_s_per_sample_batch1024": t_qb / 1024,
             "plain_gpu_sam_s": t_plain, "speedup_vs_plain_batch1": t_plain / t_q1,

@@ -21,6 +21,7 @@ HGB_ERR_INVALID_ARGUMENT = 1
 HGB_ERR_CUDA = 2
 HGB_ERR_WORKSPACE = 3
 HGB_ERR_CAPACITY = 4
+HGB_ERR_DEVICE_LIMIT = 5
 
 STATUS_ITERATION_LIMIT = 1
 STATUS_INVALID_REDSHIFT = 2
@@ -149,6 +150,7 @@ SIGNATURES = [
     ("hgb_mlp_weight_count", _l, [ctypes.POINTER(HgbMlp)]),
     ("hgb_mlp_forward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _p]),
     ("hgb_mlp_forward_fused", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p]),
+    ("hgb_emulator_query", _i, [ctypes.POINTER(HgbMlp), _p, _i, _i, _p, _p, _p, _p, _i, _p, _p, _p, _p, _p]),
     ("hgb_mlp_backward_workspace_bytes", _sz, [ctypes.POINTER(HgbMlp), _i]),
     ("hgb_mlp_backward", _i, [ctypes.POINTER(HgbMlp), _p, _l, _i, _p, _p, _p, _p, _l, _p, _p, _p, _sz, _p, _p]),
     ("hgb_mlp_adamw", _i, [ctypes.POINTER(HgbMlp), _p, _p, _p, _p, _p, _i, ctypes.c_float, ctypes.c_float,
@@ -217,7 +219,7 @@ KERNELS_PER_CALL = {
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_2pwl_phase_f32": 1, "hgb_dbn_gw": 1,
     "hgb_integrate_3dx1d": 1, "hgb_char_strain_sq": 1, "hgb_number_and_strain": 1, "hgb_number_and_strain_f32": 1, "hgb_argsort_f0_desc": 25, "hgb_argsort_f0_desc_static": 25,
     "hgb_loudest_hc_from_sorted": 7, "hgb_loudest_hc_from_sorted_ex": 7, "hgb_sam_poisson_gwb": 3, "hgb_param_grids": 1, "hgb_model_details": 9,
-    "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1, "hgb_mlp_forward_fused": 1,
+    "hgb_loudest_hc_and_par_from_sorted": 6, "hgb_mlp_adamw": 1, "hgb_mlp_pack_weights": 1, "hgb_mlp_forward_fused": 1, "hgb_emulator_query": 1,
 }
 _launches = [0]
 _launch_lock = threading.Lock()

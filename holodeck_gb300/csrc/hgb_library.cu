@@ -91,6 +91,7 @@ const char *hgb_error_string(int code) {
         case HGB_ERR_CUDA: return "CUDA error";
         case HGB_ERR_WORKSPACE: return "workspace too small";
         case HGB_ERR_CAPACITY: return "input exceeds the static scratch capacity";
+        case HGB_ERR_DEVICE_LIMIT: return "a bounded device wait gave up; outputs not valid";
         default: return "unknown error";
     }
 }

@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include <cooperative_groups.h>
 
@@ -900,6 +901,45 @@ int hgb_mlp_forward_fused(const hgb_mlp *net, const uint16_t *x, long x_member_s
     dim3 grid(FUSED_CL, (unsigned)v.E);
     k_mlp_fwd_fused<<<grid, FUSED_THREADS, smem, (cudaStream_t)stream>>>(fa);
     return hgb::check_launch();
+}
+
+int hgb_emulator_query(const hgb_mlp *net, const double *params, int n_queries, int n_params, const double *lo,
+                       const double *hi, const double *mu, const double *sd, int n_out, uint16_t *x_host,
+                       float *out_host, int *status_host, double *result, void *stream) {
+    HGB_CHECK_ARG(check_net(net) && params && lo && hi && mu && sd && x_host && out_host && status_host && result);
+    HGB_CHECK_ARG(n_queries >= 1 && n_queries <= HGB_MLP_FUSED_MAX_BATCH && n_params >= 1);
+    HGB_CHECK_ARG(n_params <= net->dims[0] && n_out >= 1 && n_out <= net->dims[net->n_layers]);
+    const int K0 = net->dims[0], NL = net->dims[net->n_layers], E = net->n_members;
+    // inputs: 2 (p - lo) / (hi - lo) - 1 rounded to float, then to bf16 (nearest, ties to even)
+    for (int q = 0; q < n_queries; q++)
+        for (int k = 0; k < K0; k++) {
+            uint16_t bits = 0;
+            if (k < n_params) {
+                const double u = (params[(long)q * n_params + k] - lo[k]) / (hi[k] - lo[k]);
+                const float f = (float)(2.0 * u - 1.0);
+                uint32_t w;
+                memcpy(&w, &f, sizeof(w));
+                bits = (uint16_t)((w + 0x7FFFu + ((w >> 16) & 1u)) >> 16);
+            }
+            x_host[(long)q * K0 + k] = bits;
+        }
+    *(volatile int *)status_host = 0;
+    int rc = hgb_mlp_forward_fused(net, x_host, 0, n_queries, out_host, status_host, stream);
+    if (rc) return rc;
+    cudaError_t err = cudaStreamSynchronize((cudaStream_t)stream);
+    if (err != cudaSuccess) {
+        hgb::set_cuda_error(err);
+        return HGB_ERR_CUDA;
+    }
+    if (*(volatile int *)status_host) return HGB_ERR_DEVICE_LIMIT;
+    // the ensemble mean in the statistics' units: mean over members, then * sd + mu
+    for (int q = 0; q < n_queries; q++)
+        for (int k = 0; k < n_out; k++) {
+            double acc = 0.0;
+            for (int e = 0; e < E; e++) acc += (double)out_host[((long)e * n_queries + q) * NL + k];
+            result[(long)q * n_out + k] = acc / E * sd[k] + mu[k];
+        }
+    return HGB_OK;
 }
 
 size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch) {

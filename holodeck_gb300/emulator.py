@@ -352,6 +352,19 @@ class Emulator:
             self._graphs[key] = g
         return g
 
+    def native(self, batch=1):
+        """The lowest-latency query path for up to ``batch`` (<= ``_native.MLP_FUSED_MAX_BATCH``) rows:
+        one call of ``hgb_emulator_query``, which maps the parameters into the box, rounds them to
+        bf16 in pinned memory, runs the fused forward on the current stream, synchronises and forms
+        the scaled ensemble mean on the host thread.  Returns a callable params (Q <= batch, P) ->
+        ensemble-mean statistics (Q, F, 4); it raises NativeError if the kernel's bounded wait gave up."""
+        key = ("native", int(batch))
+        q = self._graphs.get(key)
+        if q is None:
+            q = _NativeQuery(self, batch)
+            self._graphs[key] = q
+        return q
+
     def state(self):
         rs = getattr(self, "residual_scatter", None)
         extra = {} if rs is None else dict(residual_scatter=rs)
@@ -429,6 +442,39 @@ class _GraphedForward:
         self.emu.net.check_status(int(self.h_status_np[0]))
         out = self.h_out_np[:, :q, :self.emu.n_out].mean(axis=0, dtype=np.float64) * self.emu.sd + self.emu.mu
         return out.reshape(q, self.emu.nfreqs, 4)
+
+
+class _NativeQuery:
+    def __init__(self, emu, batch):
+        t = D.torch()
+        if not 1 <= int(batch) <= N.MLP_FUSED_MAX_BATCH:
+            raise ValueError(f"batch must be in [1, {N.MLP_FUSED_MAX_BATCH}]")
+        self.emu, self.batch = emu, int(batch)
+        net = emu.net
+        self.h_x = t.zeros((self.batch, net.dims[0]), dtype=t.int16).pin_memory()
+        self.h_out = t.zeros((net.members, self.batch, net.dims[-1]), dtype=t.float32).pin_memory()
+        self.h_status = t.zeros(1, dtype=t.int32).pin_memory()
+        self.lo = np.ascontiguousarray(emu.lo, dtype=np.float64)
+        self.hi = np.ascontiguousarray(emu.hi, dtype=np.float64)
+        self.mu = np.ascontiguousarray(emu.mu, dtype=np.float64)
+        self.sd = np.ascontiguousarray(emu.sd, dtype=np.float64)
+        self.result = np.zeros((self.batch, emu.n_out), dtype=np.float64)
+        self.fn = N.load().hgb_emulator_query
+        self.args = [ctypes.byref(net.struct), None, 0, len(self.lo)] + [
+            v.ctypes.data_as(ctypes.c_void_p) for v in (self.lo, self.hi, self.mu, self.sd)] + [
+            emu.n_out, N.ptr(self.h_x), N.ptr(self.h_out), N.ptr(self.h_status),
+            self.result.ctypes.data_as(ctypes.c_void_p)]
+
+    def __call__(self, params):
+        p = np.ascontiguousarray(np.atleast_2d(params), dtype=np.float64)
+        nq = p.shape[0]
+        if nq > self.batch or p.shape[1] != len(self.lo):
+            raise ValueError(f"at most {self.batch} rows of {len(self.lo)} parameters")
+        args = list(self.args)
+        args[1] = p.ctypes.data_as(ctypes.c_void_p)
+        args[2] = nq
+        N.check(self.fn(*args, N.stream_handle()), "hgb_emulator_query")
+        return self.result[:nq].reshape(nq, self.emu.nfreqs, 4).copy()
 
 
 def sample_statistics(res):

@@ -33,6 +33,7 @@ extern "C" {
 #define HGB_ERR_CUDA 2
 #define HGB_ERR_WORKSPACE 3
 #define HGB_ERR_CAPACITY 4   /* input larger than a static scratch array holds */
+#define HGB_ERR_DEVICE_LIMIT 5   /* a bounded device wait gave up: the call's outputs are not valid */
 
 /* ---- device status bits (OR-ed into *d_status) */
 #define HGB_STATUS_ITERATION_LIMIT 1   /* a bounded sampling / root-finding loop ran out */
@@ -457,6 +458,17 @@ int hgb_mlp_forward(const hgb_mlp *net, const uint16_t *x, long x_member_stride,
 #define HGB_MLP_FUSED_MAX_BATCH 16
 int hgb_mlp_forward_fused(const hgb_mlp *net, const uint16_t *x, long x_member_stride, int batch, float *out,
                           int *d_status, void *stream);
+/* No reference counterpart.  One emulator query end to end on the calling host thread, for query
+ * latency: params (HOST, [n_queries][n_params], n_queries <= HGB_MLP_FUSED_MAX_BATCH) are mapped to
+ * 2 (p - lo) / (hi - lo) - 1, rounded to bf16 into x_host ([n_queries][dims[0]], zero-padded), the
+ * fused forward runs on `stream` reading x_host and writing out_host ([member][n_queries][dims[L]])
+ * and status_host, the stream is synchronised, and result (HOST, [n_queries][n_out], double) receives
+ * mean over members of out * sd + mu for the first n_out outputs.  x_host, out_host and status_host
+ * must be pinned (device-accessible) host memory; lo, hi (n_params), mu, sd (n_out) are host arrays.
+ * Returns HGB_ERR_DEVICE_LIMIT when the kernel's bounded wait gave up (result not written). */
+int hgb_emulator_query(const hgb_mlp *net, const double *params, int n_queries, int n_params, const double *lo,
+                       const double *hi, const double *mu, const double *sd, int n_out, uint16_t *x_host,
+                       float *out_host, int *status_host, double *result, void *stream);
 size_t hgb_mlp_backward_workspace_bytes(const hgb_mlp *net, int batch);
 /* Mean-squared-error loss against target [batch][dims[n_layers]] (target_member_stride apart) of the
  * outputs of the last hgb_mlp_forward (with pre): loss[e] (may be NULL) and grad [E][P] fp32. */

@@ -292,8 +292,12 @@ def test_emulator_learns_a_library_and_beats_the_baselines(built_lib):
     g = emu.graphed(64)
     assert np.allclose(g(test.param_samples), mean, rtol=0, atol=1e-9)
     g1 = emu.graphed(1)                                    # the fused one-kernel graph (pinned I/O)
+    n1 = emu.native(1)                                     # the same kernel behind one native call
+    n4 = emu.native(4)
     for row in test.param_samples[:5]:
         assert np.allclose(g1(row[None]), emu.predict(row[None])[0], rtol=0, atol=1e-2)
+        assert np.allclose(n1(row), g1(row[None]), rtol=0, atol=1e-9)
+    assert np.allclose(n4(test.param_samples[:3]), emu.graphed(4)(test.param_samples[:3]), rtol=0, atol=1e-9)
     t_emu = EM.timed(g, test.param_samples, repeat=20) / 64
     solve = EM.sam_fallback(train, sam_shape=shape, nreals=nr, nfreqs=nf, seed=3)
     t_sam = EM.timed(solve, test.param_samples[0], repeat=3)
