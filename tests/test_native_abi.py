@@ -83,3 +83,44 @@ def test_schedule_knob_and_mlp_descriptions_checked_on_the_host(built_lib):
     none = N.HgbMlp()
     none.n_layers, none.n_members = 0, 1
     assert lib.hgb_mlp_param_count(ctypes.byref(none)) == -1
+
+
+def test_batch_and_query_entry_points_check_arguments_on_the_host(built_lib):
+    """The multi-sample realization launch, the fused forward and the native emulator query reject
+    bad arguments before any CUDA call (no device pointer is dereferenced here)."""
+    from holodeck_gb300 import _native as N
+    lib = N.load()
+    p = 256   # a non-null address that is never dereferenced: the checks return first
+    ok = N.HgbLoudestSample(p, p, p, 100, 10, 1, p, p, p, 1 << 30, None)
+    arr = (N.HgbLoudestSample * 1)(ok)
+    bad = N.HgbLoudestSample(None, p, p, 100, 10, 1, p, p, p, 1 << 30, None)   # no number
+    rc = lib.hgb_loudest_hc_batch((N.HgbLoudestSample * 1)(bad), 1, 4, 2, 0, p, 1 << 20, None)
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    rc = lib.hgb_loudest_hc_batch(arr, 1, 4, 2, 7, p, 1 << 20, None)           # blocks_per_sm above 6
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    rc = lib.hgb_loudest_hc_batch(arr, 1, 4, 256, 0, p, 1 << 20, None)         # nloud above 255
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    small = N.HgbLoudestSample(p, p, p, 100, 10, 1, p, p, p, 16, None)          # workspace too small
+    rc = lib.hgb_loudest_hc_batch((N.HgbLoudestSample * 1)(small), 1, 4, 2, 0, p, 1 << 20, None)
+    assert rc == N.HGB_ERR_WORKSPACE
+    rc = lib.hgb_loudest_hc_batch(arr, 1, 4, 2, 0, p, 16, None)                 # batch workspace too small
+    assert rc == N.HGB_ERR_WORKSPACE
+    assert lib.hgb_loudest_batch_workspace_bytes(arr, 1, 4) > 0
+    net = N.HgbMlp()
+    net.n_layers, net.n_members = 2, 2
+    for ii, d in enumerate((16, 32, 16)):
+        net.dims[ii] = d
+    net.params, net.weights = p, p
+    rc = lib.hgb_mlp_forward_fused(ctypes.byref(net), p, 0, N.MLP_FUSED_MAX_BATCH + 1, p, None, None)
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    net.weights = p + 8                                                        # not 16-byte aligned
+    rc = lib.hgb_mlp_forward_fused(ctypes.byref(net), p, 0, 1, p, None, None)
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    net.weights = p
+    rc = lib.hgb_emulator_query(ctypes.byref(net), p, N.MLP_FUSED_MAX_BATCH + 1, 6, p, p, p, p, 10, p, p, p, p, None)
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    rc = lib.hgb_emulator_query(ctypes.byref(net), p, 1, 17, p, p, p, p, 10, p, p, p, p, None)   # > dims[0]
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    rc = lib.hgb_emulator_query(ctypes.byref(net), p, 1, 6, p, p, p, p, 17, p, p, p, p, None)    # > dims[L]
+    assert rc == N.HGB_ERR_INVALID_ARGUMENT
+    assert lib.hgb_error_string(N.HGB_ERR_DEVICE_LIMIT).startswith(b"a bounded device wait gave up")
