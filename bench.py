@@ -367,13 +367,15 @@ def run_gpu(args):
     grid_stages = grid_stage_rooflines(H, C, fe, args.precision, n_sm, sm_mhz)
 
     batched = run_batched(args, rank, world) if args.batched_samples > 0 else None
+    # the single-GPU legs (high-resolution model, emulator) run at N = 1 only: under torchrun the
+    # other GPUs would wait idle for them
     highres = None
-    if args.highres_steps > 0 and rank == 0:
+    if args.highres_steps > 0 and world == 1:
         hargs = argparse.Namespace(**vars(args))
         hargs.steps = args.highres_steps
         highres = run_highres(hargs)
         torch.cuda.empty_cache()
-    emulator = run_emulator(args) if (args.emulator_samples > 0 and rank == 0) else None
+    emulator = run_emulator(args) if (args.emulator_samples > 0 and world == 1) else None
     cpu = hc_error = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, keep = cpu_baseline_sample(args)
