@@ -16,6 +16,8 @@
 // reference loops; the remaining differences are the last-ulp behaviour of pow/log10.
 #include <math.h>
 
+#include <algorithm>
+
 #include "hgb_common.cuh"
 
 namespace {
@@ -215,7 +217,15 @@ struct Dbn2plArgs {
     PowPlan p_outer, p_inner;   // exponents -go + gi and gi - 1 of the hardening rate
 };
 
-__global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ fobs,
+// Several (mtot, mrat) cells per block (`cpb`, chosen by the host so that cpb x n_redz rows nearly
+// fill the block): a cell's redshift rows alone would leave most of a warp idle (101 rows are three
+// warps and five lanes), and GB300 charges an FP64 warp instruction in full however few lanes are
+// active.  Row r of the block is redshift r % n_redz of the block's cell r / n_redz; each cell's step
+// tables live in its own slice of shared memory, built by the whole block.  Each row's arithmetic is
+// the single-cell kernel's.
+constexpr int WALK_MAX_CELLS = 16;
+
+__global__ void __launch_bounds__(512) k_dbn_2pwl(CyConst cc, Dbn2plArgs a, int cpb, const double *__restrict__ fobs,
                            const double *__restrict__ hard_norm, const double *__restrict__ nden,
                            const double *__restrict__ mtot, const double *__restrict__ mrat,
                            const double *__restrict__ redz, const double *__restrict__ gmt_time,
@@ -224,21 +234,19 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
                            double *__restrict__ diff_num) {
     extern __shared__ double smem[];
     const int S = a.num_steps, NI = a.n_interp, NF = a.n_freq;
+    const int ncell = a.n_mtot * a.n_mrat;
+    const int cell0 = blockIdx.x * cpb;
+    const int nc = min(cpb, ncell - cell0);   // cells of this block
     double *zg = smem;
     double *ag = zg + NI;
     double *dg = ag + NI;
-    double *ft = dg + NI;
-    double *sepa = ft + NF;          // [S+1]
-    double *frst = sepa + (S + 1);   // [S+1]
-    double *dadt = frst + (S + 1);   // [S+1]
-    double *dts = dadt + (S + 1);    // [S]
-    double *tevo = dts + S;          // [S]
-    double *sz = tevo + S;           // [NI] dz/dt of each age-table interval
-
-    int cell = blockIdx.x;
-    int ii = cell / a.n_mrat, jj = cell % a.n_mrat;
-    double mt = mtot[ii], mr = mrat[jj];
-    double norm = hard_norm[cell];
+    double *sz = dg + NI;            // [NI] dz/dt of each age-table interval
+    double *ft = sz + NI;
+    double *cells = ft + NF;         // per cell: sepa [S+1], frst [S+1], dadt [S+1], dts [S], tevo [S]
+    const int per_cell = 3 * (S + 1) + 2 * S;
+    __shared__ double s_fmax;
+    __shared__ int s_first[WALK_MAX_CELLS];
+    __shared__ double s_sqrt_mt[WALK_MAX_CELLS], s_mt3[WALK_MAX_CELLS], s_mr12[WALK_MAX_CELLS];
 
     for (int i = threadIdx.x; i < NI; i += blockDim.x) {
         zg[i] = zgrid_g[i];
@@ -248,22 +256,33 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
     for (int i = threadIdx.x; i < NF; i += blockDim.x) ft[i] = fobs[i];
     __syncthreads();
     for (int i = threadIdx.x; i < NI - 1; i += blockDim.x) sz[i] = (zg[i + 1] - zg[i]) / (ag[i + 1] - ag[i]);
-    double risco = 3.0 * HGB_CY_SCHW * mt;
-    double dx = (a.sepa_init_log10 - log10(risco)) / S;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < nc) {   // log10 separation nodes by repeated subtraction, one thread per cell
+        const int cell = cell0 + threadIdx.x;
+        const double mt = mtot[cell / a.n_mrat];
+        double *sepa = cells + (size_t)threadIdx.x * per_cell;
+        const double risco = 3.0 * HGB_CY_SCHW * mt;
+        const double dx = (a.sepa_init_log10 - log10(risco)) / S;
         double sl = a.sepa_init_log10;
         sepa[0] = sl;
         for (int s = 1; s <= S; s++) {
             sl -= dx;
             sepa[s] = sl;
         }
+        const double mr = mrat[cell % a.n_mrat];
+        s_sqrt_mt[threadIdx.x] = sqrt(mt);
+        s_mt3[threadIdx.x] = pow(mt, 3.0);
+        s_mr12[threadIdx.x] = pow(1.0 + mr, 2.0);
     }
     __syncthreads();
     // per node: sp^1.5 as sp sqrt(sp), the hardening model's (half-)integer powers as products
     // (pow_planned), and the GW rate with the cell's mt^3 and (1 + mr)^2 taken once: each within a
     // few ulp of the pow() forms of sam_cyutils.pyx:240-253 and holodeck/cyutils.pyx
-    const double sqrt_mt = sqrt(mt), mt3 = pow(mt, 3.0), mr12 = pow(1.0 + mr, 2.0);
-    for (int s = threadIdx.x; s <= S; s += blockDim.x) {
+    for (int i = threadIdx.x; i < nc * (S + 1); i += blockDim.x) {
+        const int c = i / (S + 1), s = i % (S + 1), cell = cell0 + c;
+        const double mr = mrat[cell % a.n_mrat], norm = hard_norm[cell];
+        const double sqrt_mt = s_sqrt_mt[c], mt3 = s_mt3[c], mr12 = s_mr12[c];
+        double *sepa = cells + (size_t)c * per_cell;
+        double *frst = sepa + (S + 1), *dadt = frst + (S + 1);
         const double sp = pow(10.0, sepa[s]);
         sepa[s] = sp;
         frst[s] = cc.kfreq * sqrt_mt / (sp * sqrt(sp));
@@ -273,39 +292,47 @@ __global__ void k_dbn_2pwl(CyConst cc, Dbn2plArgs a, const double *__restrict__ 
         dadt[s] = dd;
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < S; s += blockDim.x) dts[s] = 2.0 * (sepa[s + 1] - sepa[s]) / (dadt[s] + dadt[s + 1]);
+    for (int i = threadIdx.x; i < nc * S; i += blockDim.x) {
+        const int c = i / S, s = i % S;
+        double *sepa = cells + (size_t)c * per_cell;
+        const double *dadt = sepa + 2 * (S + 1);
+        double *dts = sepa + 3 * (S + 1);
+        dts[s] = 2.0 * (sepa[s + 1] - sepa[s]) / (dadt[s] + dadt[s + 1]);
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // Steps that cannot bracket any target are skipped without changing a result: the observed
+    // frequency of a step is at most its rest-frame frequency (z >= 0 after clamping) and at least
+    // frst / (1 + z_start), because the redshift only decreases from the starting redshift.
+    double fmin_all = ft[0], fmax_all = ft[0];
+    for (int f = 1; f < NF; f++) {
+        fmin_all = fmin_all < ft[f] ? fmin_all : ft[f];
+        fmax_all = fmax_all > ft[f] ? fmax_all : ft[f];
+    }
+    if (threadIdx.x < nc) {   // running time and first useful step, one thread per cell
+        double *sepa = cells + (size_t)threadIdx.x * per_cell;
+        const double *frst = sepa + (S + 1), *dts = sepa + 3 * (S + 1);
+        double *tevo = sepa + 3 * (S + 1) + S;
         double te = 0.0;
         for (int s = 0; s < S; s++) {
             te += dts[s];
             tevo[s] = te;
         }
-    }
-    __syncthreads();
-
-    // Steps that cannot bracket any target are skipped without changing a result: the observed
-    // frequency of a step is at most its rest-frame frequency (z >= 0 after clamping) and at least
-    // frst / (1 + z_start), because the redshift only decreases from the starting redshift.
-    __shared__ double s_fmax;
-    __shared__ int s_first;
-    if (threadIdx.x == 0) {
-        double fmin = ft[0], fmax = ft[0];
-        for (int f = 1; f < NF; f++) {
-            fmin = fmin < ft[f] ? fmin : ft[f];
-            fmax = fmax > ft[f] ? fmax : ft[f];
-        }
         int first = 0;   // first step whose right edge reaches fmin
-        while (first < S && frst[first + 1] < fmin) first++;
-        s_fmax = fmax;
-        s_first = first;
+        while (first < S && frst[first + 1] < fmin_all) first++;
+        s_first[threadIdx.x] = first;
+        if (threadIdx.x == 0) s_fmax = fmax_all;
     }
     __syncthreads();
     const double fmax = s_fmax;
-    const int s_begin = s_first;
 
     const double age_universe = ag[NI - 1];
-    for (int kk = threadIdx.x; kk < a.n_redz; kk += blockDim.x) {
+    for (int r = threadIdx.x; r < nc * a.n_redz; r += blockDim.x) {
+        const int c = r / a.n_redz, kk = r % a.n_redz;
+        const int cell = cell0 + c;
+        const double *frst = cells + (size_t)c * per_cell + (S + 1);
+        const double *dts = cells + (size_t)c * per_cell + 3 * (S + 1);
+        const double *tevo = dts + S;
+        const int s_begin = s_first[c];
         long row = ((long)cell * a.n_redz + kk);
         double *rf = redz_final + row * NF;
         double *dn = diff_num + row * NF;
@@ -827,14 +854,20 @@ int hgb_dbn_2pwl_phase(const double *fobs_orb, int n_freq, int fobs_sorted, doub
                  pow_plan(gamma_inner - 1.0)};
     unsigned blocks = (unsigned)((long)n_mtot * n_mrat);
     if (phase & 1) {
-        size_t smem = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq + 3 * (size_t)(num_steps + 1) +
-                                        2 * (size_t)num_steps);
-        HGB_CHECK_ARG(smem <= 200 * 1024);
+        // cells per block: fill up to 512 rows (cpb x n_redz), within a shared-memory budget
+        const size_t base = sizeof(double) * ((size_t)4 * cosmo->grid_size + n_freq);
+        const size_t per_cell = sizeof(double) * (3 * (size_t)(num_steps + 1) + 2 * (size_t)num_steps);
+        HGB_CHECK_ARG(base + per_cell <= 200 * 1024);
+        int cpb = 512 / n_redz;
+        cpb = std::min<long>(cpb, (long)((160 * 1024 - std::min<size_t>(base, 160 * 1024)) / per_cell));
+        cpb = std::max(1, std::min(cpb, WALK_MAX_CELLS));
+        const size_t smem = base + per_cell * cpb;
         int src = hgb::ensure_dyn_smem((const void *)k_dbn_2pwl, smem);
         if (src) return src;
-        int threads = ((n_redz + 31) / 32) * 32;
-        if (threads > 256) threads = 256;
-        k_dbn_2pwl<<<blocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, fobs_orb, hard_norm, nden,
+        int threads = (int)hgb::ceil_div((long)cpb * n_redz, 32) * 32;
+        if (threads > 512) threads = 512;
+        const unsigned wblocks = (unsigned)hgb::ceil_div((long)n_mtot * n_mrat, cpb);
+        k_dbn_2pwl<<<wblocks, threads, smem, (cudaStream_t)stream>>>(hgb::cy_const(), a, cpb, fobs_orb, hard_norm, nden,
                                                                     mtot, mrat, redz, gmt_time, cosmo->grid_z,
                                                                     cosmo->grid_age, cosmo->grid_dcom, redz_final,
                                                                     diff_num);
