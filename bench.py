@@ -254,6 +254,15 @@ def grid_stage_rooflines(H, C, fe, precision, n_sm, sm_mhz):
                      "FP64-pipe utilisation of the iterative grid kernels is in profiles/")}
 
 
+def emit(args, obj):
+    """Print one result line (the bench contract) and, with --json-out, append it to that file."""
+    text = json.dumps(obj)
+    print(text, flush=True)
+    if getattr(args, "json_out", None):
+        with open(args.json_out, "a") as fh:
+            fh.write(text + "\n")
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -409,7 +418,7 @@ def run_gpu(args):
             "highres": highres,
             "emulator": emulator,
         }
-        print(json.dumps(line))
+        emit(args, line)
     if world > 1:
         dist.destroy_process_group()
 
@@ -731,7 +740,7 @@ def run_reference(args):
                              "note": ("ms_per_step is the wall time per sampled evaluation with every core busy; "
                                       "value extrapolates each sample to the workload's 1000 realizations")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    emit(args, line)
 
 
 def run_profile(args):
@@ -895,21 +904,22 @@ def main():
                     help="timed evaluations of the high-resolution measurement carried by the bench line (0: skip)")
     ap.add_argument("--highres", action="store_true",
                     help="only the high-resolution workload (181x161x201, 100 frequencies, 10^4 realizations)")
+    ap.add_argument("--json-out", default=None, help="also append each result line to this file")
     ap.add_argument("--emulator-cache", default=None,
                     help=".npz holding the emulator's training library statistics (written when absent)")
     args = ap.parse_args()
     if args.batched and args.impl != "reference":
         import torch
         torch.cuda.set_device(dist_env()[2])
-        print(json.dumps({"metric": METRIC, "batched": run_batched(args)}))
+        emit(args, {"metric": METRIC, "batched": run_batched(args)})
     elif args.emulator and args.impl != "reference":
         import torch
         torch.cuda.set_device(dist_env()[2])
-        print(json.dumps({"metric": METRIC, "emulator": run_emulator(args)}))
+        emit(args, {"metric": METRIC, "emulator": run_emulator(args)})
     elif args.highres:
         import torch
         torch.cuda.set_device(dist_env()[2])
-        print(json.dumps({"metric": METRIC, "highres": run_highres(args)}))
+        emit(args, {"metric": METRIC, "highres": run_highres(args)})
     elif args.mlp_profile:
         run_mlp_profile(args)
     elif args.profile:
