@@ -88,7 +88,7 @@ constexpr int MAX_INVERSION = 4096;
 constexpr int MAX_PREFIX_EXTRA = 1024;   // prefix events beyond L (Normal draws below 1)
 constexpr double TABLE_MAX = 47000.0;    // table inversion up to here: k_lo..k_hi spans <= 14 sqrt(lambda) + 10
 constexpr int TMAX = 3072;               // table entries (>= 14 sqrt(TABLE_MAX) + 10 = 3046)
-constexpr int HALF_WORDS = 1536 + 1024;  // tables up to 1536 entries (2^11 u16 guide cells) fit a half
+constexpr int HALF_WORDS = 2048 + 512;   // tables up to 2048 entries (2^10 u16 guide cells) fit a half
 constexpr int ARENA_WORDS = 2 * HALF_WORDS;   // the halves alternate between build and draw
 static_assert(TMAX + 2048 <= ARENA_WORDS, "the largest table (2^12 guide cells) fits the whole arena");
 constexpr int BATCH_MAX = 32;            // table-kind bins built per batch
@@ -293,7 +293,7 @@ __device__ void bin_setup(Tile &s, int j, int kind, double lam, double h) {
             const int S = min((int)ceilf(lf + TABLE_SIGMAS * sd + 6.0f) - k_lo + 1, TMAX);
             s.tb_klo[j] = k_lo;
             s.tb_S[j] = S;
-            s.tb_gb[j] = 32 - __clz(S - 1);   // ceil(log2 S): 2^gb >= S guide cells, S >= 2
+            s.tb_gb[j] = max(1, 31 - __clz(S - 1));   // ceil(log2 S) - 1: 2^gb >= S / 2 guide cells
         }
     }
 }
@@ -759,7 +759,12 @@ struct BulkArgs {
 //              (rounded to nearest); cdf[S - 1] = 2^32 - 1, so the mass outside the range (< 1e-11)
 //              goes to the end entries;
 //   guide[c] = m | flags, m (bits 0-11) the smallest entry with cdf[m] > c 2^(32 - gb), for the
-//              2^gb >= S cells; GUIDE_PURE when cdf[m] >= (c + 1) 2^(32 - gb), so every u in the cell
+//              2^gb >= S / 2 cells: about one cell per two entries.  Against 2^gb >= S cells the
+//              draws cost more (more cells hold several boundaries), but the guide builds faster,
+//              tables up to 2048 entries fit half the arena (one warp builds them, not the block) and
+//              more tables share a batch barrier: on the bench workload k_bulk takes 27.5 ms against
+//              28.9 ms (2^gb >= S / 4: 28.3 ms).  GUIDE_PURE when cdf[m] >= (c + 1) 2^(32 - gb), so
+//              every u in the cell
 //              maps to m; GUIDE_ONE when instead cdf[m + 1] >= (c + 1) 2^(32 - gb), so u maps to m or
 //              m + 1 by one comparison; neither: two or more entries end inside the cell (a "tail"
 //              cell of the distribution), resolved by a binary search between guide[c] and
