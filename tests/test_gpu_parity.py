@@ -259,9 +259,9 @@ def test_philox_poisson_statistics(built_lib):
     from holodeck_gb300 import cyutils
     from scipy import stats
     # sampler boundaries: sparse 0.1, alias 10, inversion tables up to 47000 (one warp builds a table of
-    # up to 1536 entries, lambda about 11500, the whole block above), PTRS32 above, PTRS64 beyond 2^22
+    # up to 2048 entries, lambda about 21200, the whole block above), PTRS32 above, PTRS64 beyond 2^22
     lams = np.array([1e-7, 0.03, 0.099, 0.1, 0.12, 0.16, 0.7, 3.0, 9.99, 10.0, 37.5, 412.0, 1500.0, 2000.0, 2100.0,
-                     3000.0, 1.15e4, 1.16e4, 4.69e4, 4.71e4, 6.0e4, 9.1e4, 5.0e6])
+                     3000.0, 1.15e4, 1.16e4, 2.1e4, 2.2e4, 4.69e4, 4.71e4, 6.0e4, 9.1e4, 5.0e6])
     nreals = 20000
     # one bin per lambda, one frequency; L=0 so every source goes to the background sum
     number = lams.reshape(-1, 1, 1, 1)
