@@ -188,8 +188,14 @@ def _run_jobs(space, jobs, workers, nfreqs, nloudest, pta_dur, flags, reduce=Non
                 _save_sim_file(sim_fname(output_dir, job.index), space, job, res, err)
             except OSError as exc:
                 err = err or exc
+        value = None
+        if err is None:
+            try:   # a failing reduce fails its sample, not the thread that runs it
+                value = res if reduce is None else reduce(res)
+            except Exception as exc:
+                err = exc
         with lock:
-            results[job.index] = None if err is not None else (res if reduce is None else reduce(res))
+            results[job.index] = value
             if err is not None:
                 errors[job.index] = err
                 if max_failures is not None and len(errors) > max_failures:

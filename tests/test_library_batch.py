@@ -252,3 +252,27 @@ def test_failed_sample_is_isolated_and_resumed(built_lib, tmp_path):
     assert np.array_equal(again[2]["hc_ss"], clean[2]["hc_ss"]) and np.array_equal(again[2]["hc_bg"], clean[2]["hc_bg"])
     with pytest.raises(RuntimeError, match="max_failures"):
         batch.run_library(_FailingSpace(space, 1), shapes, nreals, max_failures=0, **kw)
+
+
+@pytest.mark.gpu
+def test_failing_reduce_fails_only_its_sample(built_lib, monkeypatch):
+    """A caller's ``reduce`` that raises for one sample marks that sample failed; the others finish
+    (the worker thread survives)."""
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform, batch
+    space = PS_Classic_Phenom_Uniform(nsamples=5, seed=4)
+
+    def fake_run_model(sam, hard, nreals=1, **kw):
+        return dict(hc_bg=np.full((2, nreals), 1.0))
+
+    monkeypatch.setattr(batch, "run_model", fake_run_model)
+    monkeypatch.setattr(space, "model_for_params", lambda params, shape: (None, None))
+
+    def reduce(res):
+        if res["hc_bg"].shape[1] == 3:
+            raise ValueError("bad sample")
+        return float(res["hc_bg"].sum())
+
+    jobs = batch.make_jobs(space, (10, 10, 10), [1, 2, 3, 4, 5])
+    results, errors = batch._run_jobs(space, jobs, 2, 2, 1, 16.0, dict(singles_flag=True), reduce=reduce)
+    assert set(errors) == {2} and isinstance(errors[2], ValueError)
+    assert results[2] is None and [results[i] for i in (0, 1, 3, 4)] == [2.0, 4.0, 8.0, 10.0]
