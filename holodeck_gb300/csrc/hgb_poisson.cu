@@ -1062,6 +1062,21 @@ __device__ __forceinline__ void bulk_block(const BulkArgs &a, const ParArgs &pa,
         // whole block.  Four realizations per Philox call.
         const int n_table = kind_count(s, KIND_TABLE);
         if (n_table > 0) {
+            // largest tables first: big tables come in batches of their own and the many small ones
+            // share later batches, where the warps' builds balance (rank sort of the tile's list;
+            // the draws are keyed by bin, so only the summation order of the background changes)
+            int jt = 0, rank = 0;
+            if (t < n_table) {
+                jt = s.list[KIND_TABLE][t];
+                const int St = s.tb_S[jt];
+                for (int u = 0; u < n_table; u++) {
+                    const int Su = s.tb_S[s.list[KIND_TABLE][u]];
+                    rank += (Su > St || (Su == St && u < t)) ? 1 : 0;
+                }
+            }
+            __syncthreads();   // every entry is read before any is moved
+            if (t < n_table) s.list[KIND_TABLE][rank] = (unsigned char)jt;
+            __syncthreads();   // the sorted list is complete before any batch is formed
             int li = 0;
             int cur_li = 0, cur_K = 0, cur_half = 0;
             bool cur_big = false;
