@@ -153,16 +153,17 @@ def device_cosmology(cosmo, dev=None):
 _SIDE_STREAMS = {}
 
 
-def side_stream(role, dev=None):
+def side_stream(role, dev=None, priority=0):
     """A second stream for grid stages that overlap the calling thread's current stream: one per
     (device, current stream, role), so host workers that each run on their own stream never share
-    one."""
+    one.  ``priority`` -1 makes the block scheduler start this stream's blocks first as SMs free up
+    (CUDA stream priorities; 0 is the default and lowest)."""
     t = torch()
     cur = t.cuda.current_stream(device(dev))
     key = (cur.device.index, cur.cuda_stream, role)
     s = _SIDE_STREAMS.get(key)
     if s is None:
-        s = _SIDE_STREAMS.setdefault(key, t.cuda.Stream(device=cur.device))
+        s = _SIDE_STREAMS.setdefault(key, t.cuda.Stream(device=cur.device, priority=int(priority)))
     return s
 
 

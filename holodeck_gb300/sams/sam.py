@@ -194,9 +194,9 @@ class Semi_Analytic_Model:
 
     def _dbn_2pwl_overlapped(self, hard, fobs_orb, precision="fp64"):
         """_dbn_device for Fixed_Time_2PL_SAM on a fresh instance, with the separation-step walk (which
-        needs gmt_time but not the density) on a second stream while the current stream applies the
-        M-Mbulge scatter; the evaluation, which needs the final density, follows on the current
-        stream.  Same results as _dbn_device."""
+        needs gmt_time but not the density) on a second stream while a high-priority third stream
+        applies the M-Mbulge scatter; the evaluation, which needs the final density, follows on the
+        current stream.  Same results as _dbn_device."""
         t = D.torch()
         dens, gmt_time, redz_prime = self._static_density_launch()
         mt, mr, rz = self._edges_device()
@@ -211,8 +211,19 @@ class Semi_Analytic_Model:
             walk_done = t.cuda.Event()
             walk_done.record(side)
         gmt_time.record_stream(side)
-        with D.nvtx("hgb:mbulge_scatter"):
+        # the scatter's gradient solve is one latency-bound block per redshift slice: on a
+        # high-priority stream its blocks take SMs as the hardening normalisation's blocks retire,
+        # and the normalisation and the walk fill the rest
+        hi = D.side_stream("mbulge_scatter", main.device, priority=-1)
+        hi.wait_event(static_done)
+        with t.cuda.stream(hi), D.nvtx("hgb:mbulge_scatter"):
             self._scatter_finish(dens, gmt_time, redz_prime)
+            scatter_done = t.cuda.Event()
+            scatter_done.record(hi)
+        for x in (dens, gmt_time, redz_prime):
+            if x is not None:
+                x.record_stream(hi)
+        main.wait_event(scatter_done)
         main.wait_event(walk_done)
         redz_final.record_stream(main)
         diff_num.record_stream(main)
