@@ -630,7 +630,7 @@ __global__ void k_dbn_gw(CyConst cc, const double *__restrict__ fobs, int NF, co
     }
 }
 
-// The same root, one warp per cell and sixteen cells per block.  A lane holds the constants of nodes
+// The same root, one warp per cell and eight cells per block.  A lane holds the constants of nodes
 // s = lane + 32 k in registers: the hardening shape, the GW rate and the trapezoid coefficient
 // c[s] = 2 (sepa[s+1] - sepa[s]).  Each Brent round sums the lifetime c[s] / (v[s] + v[s+1]) with
 // one partial per lane and an xor-butterfly reduction.  Every lane ends with the same total
@@ -639,10 +639,10 @@ __global__ void k_dbn_gw(CyConst cc, const double *__restrict__ fobs, int NF, co
 // differs from the reference's step order (a relative change of the lifetime near 1e-16, far
 // below the 1e-3 root tolerance, which the root follows unless a Brent comparison falls within
 // that margin: the normalisation is checked against the reference at 1e-10 in log10).
-constexpr int NB_CELLS = 16;
+constexpr int NB_CELLS = 8;    // 256 threads: half an SM's registers, so other stages' blocks fit beside
 constexpr int NB_NODES = 10;   // nodes per lane: nsteps + 1 <= 320
 
-__global__ void __launch_bounds__(NB_CELLS * 32, 1) k_hardening_norm_blk(CyConst cc, NormArgs a,
+__global__ void __launch_bounds__(NB_CELLS * 32, 2) k_hardening_norm_blk(CyConst cc, NormArgs a,
                                                                        const double *__restrict__ mtot,
                                                                        const double *__restrict__ mrat, int n,
                                                                        double *__restrict__ norm_log10,
