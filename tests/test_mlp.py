@@ -311,3 +311,44 @@ def test_emulator_learns_a_library_and_beats_the_baselines(built_lib):
     cut = float(np.median(spread_q))
     _, by_spread = emu.query(q, fallback=None, max_spread=cut)
     assert list(by_spread) == list((spread_q > cut) | np.array([False, True, False]))
+
+
+def test_boundary_space_points_lie_on_faces():
+    """Every point of the boundary library has exactly one coordinate at a bound of the box, and all
+    coordinates inside it."""
+    from holodeck_gb300 import emulator as EM
+    from holodeck_gb300.librarian import PS_Classic_Phenom_Uniform
+    sp = EM.boundary_space(PS_Classic_Phenom_Uniform, 200, seed=3)
+    lo, hi = sp.extrema[:, 0], sp.extrema[:, 1]
+    p = sp.param_samples
+    assert p.shape == (200, len(sp.param_names))
+    assert np.all(p >= lo - 1e-12) and np.all(p <= hi + 1e-12)
+    on_face = np.isclose(p, lo, rtol=0, atol=1e-12) | np.isclose(p, hi, rtol=0, atol=1e-12)
+    assert np.all(on_face.sum(axis=1) == 1)
+    assert sp.param_dict(0)[sp.param_names[0]] == p[0, 0]
+
+
+def test_residual_scaled_spread_on_the_host():
+    """The residual-scaled spread divides each output's member standard deviation by
+    max(max_spread, its training-residual scatter): a noisy output no longer flags the query."""
+    from holodeck_gb300.emulator import Emulator
+    emu = Emulator.__new__(Emulator)
+    emu.nfreqs = 1
+    emu.lo, emu.hi = np.zeros(2), np.ones(2)
+    # members: output 0 (first statistic) spread 0.08 dex, the others 0.01
+    base = np.zeros((4, 1, 1, 4))
+    base[:, 0, 0, 0] = np.array([0.0, 0.16, 0.0, 0.16]) - 0.08   # std 0.08
+    base[:, 0, 0, 1:] = np.array([0.0, 0.02, 0.0, 0.02])[:, None] - 0.01
+    emu.predict_members = lambda params: base
+    q = np.array([[0.5, 0.5]])
+    _, spread, inside = emu.predict(q)
+    assert inside.all() and np.isclose(spread[0], 0.08)
+    emu.residual_scatter = np.array([0.1, 0.0, 0.0, 0.0])          # output 0 is that noisy anyway
+    _, spread_rs, _ = emu.predict(q, residual_scaled=True, max_spread=0.05)
+    assert np.isclose(spread_rs[0], 0.05 * 0.08 / 0.1)               # below the threshold: accepted
+    emu.residual_scatter = np.zeros(4)
+    _, spread_rs, _ = emu.predict(q, residual_scaled=True, max_spread=0.05)
+    assert np.isclose(spread_rs[0], 0.08)                            # the plain criterion again
+    emu.residual_scatter = None
+    with pytest.raises(ValueError):
+        emu.predict(q, residual_scaled=True)
