@@ -212,8 +212,8 @@ def check(rc, what):
     raise NativeError(f"{what}: {msg} (code {rc})")
 
 
-#: kernels each entry point launches (the radix sort is CUB's onesweep: histogram, scan and one pass
-#: per 8 key bits); used to report the launch count of a timed region
+#: kernels each entry point launches (the radix argsort: a key gather, then a count, a scan and a
+#: scatter per 8 key bits); used to report the launch count of a timed region
 KERNELS_PER_CALL = {
     "hgb_static_density": 1, "hgb_zero_stalled": 1, "hgb_add_scatter_to_masses": 5,
     "hgb_find_2pwl_hardening_norm": 1, "hgb_sqrt_inplace": 1, "hgb_dbn_2pwl": 2, "hgb_dbn_2pwl_phase": 1, "hgb_dbn_2pwl_phase_f32": 1, "hgb_dbn_gw": 1,

@@ -406,9 +406,10 @@ int hgb_bulk_timing(int enable);
 float hgb_bulk_last_ms(void);
 
 /* No reference counterpart.  Schedule knob of the realization kernels, set by the batched-library
- * autotuner: the chunk count of k_bulk aims for `waves` waves of resident blocks (six per SM) over the
- * device's SMs (default 12).  Applies to every later launch in the process; workspace sizes are
- * always computed for HGB_BULK_WAVES_MAX, so changing it never invalidates a workspace. */
+ * autotuner: the chunk count of k_bulk aims for `waves` waves of resident blocks (counted at six
+ * per SM, the kernel's launch-bounds minimum; seven fit) over the device's SMs (default 12).
+ * Applies to every later launch in the process; workspace sizes are always computed for
+ * HGB_BULK_WAVES_MAX, so changing it never invalidates a workspace. */
 #define HGB_BULK_WAVES_MAX 16
 int hgb_set_bulk_waves(int waves);   /* 1 <= waves <= HGB_BULK_WAVES_MAX, else HGB_ERR_INVALID_ARGUMENT */
 int hgb_get_bulk_waves(void);
