@@ -220,7 +220,7 @@ struct Dbn2plArgs {
 // Several (mtot, mrat) cells per block (`cpb`, chosen by the host so that cpb x n_redz rows nearly
 // fill the block): a cell's redshift rows alone would leave most of a warp idle (101 rows are three
 // warps and five lanes), and GB300 charges an FP64 warp instruction in full however few lanes are
-// active.  Row r of the block is redshift r % n_redz of the block's cell r / n_redz; each cell's step
+// active.  Row r of the block is redshift r / nc of its cell r % nc (nc cells in the block); each cell's step
 // tables live in its own slice of shared memory, built by the whole block.  Each row's arithmetic is
 // the single-cell kernel's.
 constexpr int WALK_MAX_CELLS = 16;
@@ -327,7 +327,9 @@ __global__ void __launch_bounds__(512) k_dbn_2pwl(CyConst cc, Dbn2plArgs a, int 
 
     const double age_universe = ag[NI - 1];
     for (int r = threadIdx.x; r < nc * a.n_redz; r += blockDim.x) {
-        const int c = r / a.n_redz, kk = r % a.n_redz;
+        // redshift-major: a warp's lanes hold a few neighbouring redshifts of every cell of the block
+        // (mostly one mtot, so one rest-frequency table), whose walks have similar lengths
+        const int c = r % nc, kk = r / nc;
         const int cell = cell0 + c;
         const double *frst = cells + (size_t)c * per_cell + (S + 1);
         const double *dts = cells + (size_t)c * per_cell + 3 * (S + 1);
